@@ -1,0 +1,301 @@
+"""Benchmark of the per-trial hot path on GB300.
+
+Workload (one step = one batch): the batched test-trial mix -- a fixed grown
+network of 2000 HVC(RA) and 550 HVC(I) neurons on a sphere, carrying a synfire
+chain of 20 groups x 100 neurons with 0.05 mS/cm^2 per synapse between
+consecutive groups (reference weight 500: raiseExcWeight divides by the 10000
+um^2 dendritic area), log-normal axonal delays (mean 3 ms, sd 1.5 ms, capped at
+10 ms), run as 1024 independent 500 ms test trials (trial_no_stdp_fixedSpread,
+24999 steps of 0.02 ms each) that differ only in their Philox noise streams.
+Single precision on the device; spikes are checked against the double build.
+
+value: trials/s of the device-resident batch (CUDA events).  e2e: the same
+through the C ABI with the host copies of every step's inputs and results.
+--impl reference: the CPU restatement of the reference (oracle/), on every
+host core, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_RA, N_I, GROUPS, GROUP, WEIGHT = 2000, 550, 20, 100, 500.0
+NUM_STEPS = 25000
+BATCH = 1024
+SEED = 3
+# Algorithmic SFU work per neuron-step of the single-precision integrators,
+# counted from ug_neuron.cuh: RA 4 stages x (8 ex2 + 7 rcp); I 12 stages x (7 ex2 + 4 rcp).
+MUFU_RA, MUFU_I = 60, 132
+CPU_SAMPLE_STEPS = 6000   # first 120 ms of a trial (includes the training kick at 100 ms)
+
+
+def make_network(num_steps=NUM_STEPS):
+    from unsupervised_growth_gb300.network import synthetic_chain_network
+    return synthetic_chain_network(n_ra=N_RA, n_i=N_I, n_groups=GROUPS, group_size=GROUP, weight=WEIGHT, seed=SEED,
+                                   delays="lognormal", lognormal_mean=3.0, lognormal_sigma=1.5, delay_cap=10.0,
+                                   num_steps=num_steps)
+
+
+def workload_config():
+    return {"workload": "batched test trials, 2000 HVC-RA + 550 HVC-I synfire-chain network (20x100, 0.05 mS/cm^2), "
+                        "lognormal delays mean 3 ms, 1024 Philox-seeded 500 ms trials per step",
+            "n_ra": N_RA, "n_i": N_I, "trials_per_step": BATCH, "steps_per_trial": NUM_STEPS - 1, "dt_ms": 0.02,
+            "l2": "state+rings of a batch exceed L2 (129 MB); L2 also flushed between steps"}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def _cpu_worker(args):
+    trial, steps = args
+    sys.path.insert(0, ROOT)
+    from oracle.oracle import OracleNet
+    net = make_network(num_steps=steps)
+    onet = OracleNet(net)
+    t0 = time.perf_counter()
+    onet.run_trial(False, trial)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(cores: int, steps: int = CPU_SAMPLE_STEPS):
+    """Aggregate trials/s of the oracle on `cores` processes, each integrating a
+    `steps`-step prefix of its own trial."""
+    from oracle import oracle as O
+    O.build()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        times = pool.map(_cpu_worker, [(k, steps) for k in range(cores)])
+    frac = (steps - 1) / (NUM_STEPS - 1)
+    rate = sum(frac / t for t in times)
+    return rate, times
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine, calibrate_pipes
+
+    B.build()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    net = make_network()
+    eng = Engine(precision=32, device=local_rank, spike_capacity_per_neuron=16, use_graphs=True)
+    # a dedicated stream: the engine's kernels and the timing events share it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    eng.set_stream(stream.cuda_stream)
+    rn = eng.load_network(net)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    first = rank * 1_000_000
+
+    for w in range(args.warmup):
+        rn.run_test_trials(first + w * BATCH, BATCH)
+    torch.cuda.synchronize()
+
+    launches0 = eng.launch_count()
+    step_ms = []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rn.run_test_trials(first + (args.warmup + k) * BATCH, BATCH)
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    launches = eng.launch_count() - launches0
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+
+    # e2e through the C ABI: trial list H2D, batch, per-neuron spike statistics D2H
+    e2e_s = []
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rn.run_test_trials(first + (args.warmup + args.steps + k) * BATCH, BATCH)
+        stats = [rn.trial_stats(w) for w in (0, 1, 2)]
+        e2e_s.append(time.perf_counter() - t0)
+    h2d = BATCH * (4 + 8)
+    d2h = sum(a.nbytes + b.nbytes for a, b in stats)
+    spikes_per_trial = float(stats[0][0].sum()) / BATCH
+
+    result = None
+    if rank == 0:
+        trials = BATCH * args.steps * world
+        value = trials / (total_ms / 1e3)
+        e2e_value = BATCH * args.steps * world / max(sum(e2e_s), 1e-9)
+        mufu_peak, fma_peak = calibrate_pipes(local_rank)
+        n_launch_interval = NUM_STEPS - 1
+        avg_interval = 24999 / 2000.0
+        mufu_per_launch = BATCH * (N_RA * MUFU_RA + N_I * MUFU_I) * avg_interval
+        avg_launch_ms = (sum(step_ms) / args.steps) / (2000 + 1)
+        achieved = mufu_per_launch / (avg_launch_ms * 1e-3)
+
+        # plain double-precision GPU path: one trial per run, no batching, no graph
+        eng64 = Engine(precision=64, device=local_rank, use_graphs=False)
+        rn64 = eng64.load_network(net)
+        rn64.run_test_trials(first, 1)
+        eng64.synchronize()
+        t0 = time.perf_counter()
+        rn64.run_test_trials(first, 1)
+        eng64.synchronize()
+        fp64_s = time.perf_counter() - t0
+        # accuracy of the single build against the double build on the same trial
+        from tests.helpers import match_within, sorted_spikes
+        rn.run_test_trials(first, 1)
+        acc = {}
+        for w, name in ((0, "soma"), (1, "dend"), (2, "interneuron")):
+            a = sorted_spikes(*rn.spikes(0, w))
+            b = sorted_spikes(*rn64.spikes(0, w))
+            frac, worst = match_within(a, b, 1)
+            acc[name] = {"spikes_fp32": int(len(a)), "spikes_fp64": int(len(b)), "matched_within_1_step": frac,
+                         "max_step_error": worst}
+        rn64.free()
+        eng64.close()
+
+        cores = min(os.cpu_count() or 1, 16)
+        cpu_rate, cpu_times = cpu_sample(cores) if not args.skip_cpu else (None, [])
+        result = {
+            "metric": "trials/s (500 ms test trials, 2000 RA + 550 I network)",
+            "value": value, "unit": "trials/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded network and Philox noise)",
+            "config": dict(workload_config(), parallelism=f"replicas{world}"),
+            "neuron_steps_per_s": value * (N_RA + N_I) * (NUM_STEPS - 1),
+            "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu_peak / 1e9, "unit": "GMUFU/s",
+                         "frac": achieved / mufu_peak, "traffic": None,
+                         "kernel": "k_interval<float>",
+                         "peak_source": "ex2.approx+rcp.approx throughput loop (ug_calibrate_pipes), this run",
+                         "fma_peak_gops": fma_peak / 1e9,
+                         "algorithmic_per_launch": f"{mufu_per_launch:.4g} MUFU ops"},
+            "fp64_plain_gpu": {"trials_per_s": 1.0 / fp64_s, "speedup_of_value": value * fp64_s},
+            "accuracy_vs_fp64": acc,
+            "soma_spikes_per_trial": spikes_per_trial,
+            "clocks": clk.summary(),
+        }
+        if cpu_rate is not None:
+            result["cpu_baseline"] = {"value": cpu_rate, "unit": "trials/s", "cores": cores, "kind": "port",
+                                      "sample": f"oracle/ (double-precision CPU restatement) on {cores} processes, "
+                                                f"each the first {CPU_SAMPLE_STEPS - 1} steps (120 ms) of its own "
+                                                f"trial of this network; rate scaled by the 24999-step trial"}
+    rn.free()
+    eng.close()
+    if dist:
+        dist.destroy_process_group()
+    return result
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    cores = min(os.cpu_count() or 1, 16)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        pass
+    rates = []
+    for _ in range(args.steps):
+        r, _ = cpu_sample(cores)
+        rates.append(r)
+    value = statistics.mean(rates)
+    return {"impl": "reference", "metric": "trials/s (500 ms test trials, 2000 RA + 550 I network)", "value": value,
+            "unit": "trials/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 / value if value else None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded network and Philox noise)",
+            "config": dict(workload_config(), parallelism=f"cpu{cores}"),
+            "cpu_baseline": {"value": value, "unit": "trials/s", "cores": cores, "kind": "port",
+                             "sample": f"each step: {cores} processes, each the first {CPU_SAMPLE_STEPS - 1} steps "
+                                       f"of its own trial, scaled by the 24999-step trial"},
+            "e2e": {"value": value, "unit": "trials/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
+    local_rank = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+    else:
+        res = run_ours(args, rank, world, local_rank)
+    if rank == 0 and res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

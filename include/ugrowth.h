@@ -1,0 +1,145 @@
+/*
+ * ugrowth.h -- C ABI of the GB300 trial engine for the HVC network-growth
+ * simulator (reference: Sawndip/unsupervised_growth, c++/).
+ *
+ * The reference has no FFI for this path: its per-trial hot path lives behind
+ * the C++ class NetworkGrowthSimulator (c++/include/NetworkGrowthSimulator.h),
+ * whose callers are the four command-line drivers.  Each entry point below
+ * names the reference member function it replaces.  All arrays are plain host
+ * pointers; the library copies inputs to device memory and copies outputs back.
+ * Every call returns a ug_status; ug_last_error() gives a message for the
+ * calling thread.  A context is used from one host thread at a time.
+ */
+#ifndef UGROWTH_H
+#define UGROWTH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ug_ctx ug_ctx;
+
+typedef enum {
+    UG_OK = 0,
+    UG_EINVAL = 1,      /* bad argument or inconsistent network description */
+    UG_ENOMEM = 2,      /* device allocation failed */
+    UG_EIO = 3,         /* file could not be read or written */
+    UG_ENUMERIC = 4,    /* check_bad_values failed (NetworkGrowthSimulator.cpp:4538-4551) */
+    UG_ETIMEOUT = 5,    /* a bounded device wait gave up */
+    UG_ECAPACITY = 6,   /* a fixed-capacity device buffer overflowed (spikes, events) */
+    UG_ECUDA = 7,       /* CUDA runtime error */
+    UG_ENOTSUP = 8      /* not supported by this build or device */
+} ug_status;
+
+/* SynapticParameters, c++/include/ConfigurationNetworkGrowth.h:10-33 */
+typedef struct {
+    int32_t Nss;
+    int32_t _pad;
+    double A_P, A_D, T_0, T_P, T_D, TAU_P, TAU_D;
+    double BETA, BETA_SUPERSYNAPSE;
+    double ACTIVATION_THRESHOLD, SUPERSYNAPSE_THRESHOLD, WEIGHT_MAX;
+} ug_synaptic_params;
+
+/* MaturationParameters, ConfigurationNetworkGrowth.h:36-80 (fields the path reads) */
+typedef struct {
+    double E_REST_MATURE, E_REST_IMMATURE;
+    double GCA_MATURE, GCA_IMMATURE;
+    double DEATH_RATE_THRESHOLD;
+    int32_t RATE_WINDOW_LONG;
+    int32_t _pad;
+} ug_maturation_params;
+
+/* NoiseParameters, ConfigurationNetworkGrowth.h:83-94 */
+typedef struct {
+    double white_noise_mean_soma, white_noise_std_soma;
+    double white_noise_mean_dend, white_noise_std_dend;
+} ug_noise_params;
+
+/* ConnectionParameters, ConfigurationNetworkGrowth.h:97-105, plus the spatial
+ * constants of TopologyParameters (ConfigurationNetworkTopology.h:11-21) that
+ * neuron replacement uses. */
+typedef struct {
+    double Gei_max, Gie_max, delay_constant;
+    double A_RA2I, SIGMA_RA2I, B_I2RA, SIGMA_I2RA;
+    double model_interneuron_distance;
+} ug_connection_params;
+
+/* Everything read_network_state (NetworkGrowthSimulator.cpp:1943-2020) loads,
+ * as caller-owned host arrays.  Connection lists are CSR over the source
+ * neuron in the reference's list order; RA->RA matrices are dense row-major. */
+typedef struct {
+    int32_t n_ra, n_i;
+    int32_t num_steps;          /* 25000 = TRIAL_DURATION / TIMESTEP (24999 steps) */
+    int32_t net_id;             /* selects the noise streams together with seed */
+    uint64_t seed;
+    ug_synaptic_params syn;
+    ug_maturation_params mat;
+    ug_noise_params noise;
+    ug_connection_params conn;
+    const int32_t* ra2i_off; const int32_t* ra2i_tgt; const double* ra2i_w; const double* ra2i_d; const double* ra2i_len;
+    const int32_t* i2ra_off; const int32_t* i2ra_tgt; const double* i2ra_w; const double* i2ra_d; const double* i2ra_len;
+    const double* w_rara; const double* d_rara; const double* len_rara;
+    const int32_t* active_off; const int32_t* active_tgt;
+    const int32_t* super_off; const int32_t* super_tgt;
+    const double* rest_potential; const double* gca;
+    const int32_t* mature; const double* maturation_scale;
+    const int32_t* remodeled; const int32_t* trials_after_replacement;
+    const int32_t* activity_history;   /* n_ra x RATE_WINDOW_LONG, newest first */
+    int32_t n_tr;
+    const int32_t* training; const double* training_spread;
+    const double* ra_xyz; const double* i_xyz;
+} ug_network_desc;
+
+typedef struct {
+    int32_t precision;                  /* 64: parity build, 32: production build */
+    int32_t device;                     /* CUDA device ordinal */
+    int32_t spike_capacity_per_neuron;  /* spike-record capacity per neuron and trial (0: 16) */
+    int32_t use_graphs;                 /* replay trial batches from captured CUDA graphs */
+} ug_runtime_opts;
+
+const char* ug_last_error(void);
+
+/* Replaces constructing NetworkGrowthSimulator (NetworkGrowthSimulator.cpp:48-82). */
+ug_status ug_create(ug_ctx** out, const ug_runtime_opts* opts);
+void ug_destroy(ug_ctx* ctx);
+/* Work is issued on this cudaStream_t (passed as void*); NULL = the context's own stream. */
+ug_status ug_set_stream(ug_ctx* ctx, void* stream);
+ug_status ug_synchronize(ug_ctx* ctx);
+
+/* Replaces read_network_state + initialize_network (NetworkGrowthSimulator.cpp:1943-2020, 745-890):
+ * copies the description to device memory. */
+ug_status ug_load_network(ug_ctx* ctx, const ug_network_desc* desc, int32_t* net_id);
+ug_status ug_free_network(ug_ctx* ctx, int32_t net_id);
+
+/* Replaces the trial loop of test_chain (NetworkGrowthSimulator.cpp:1395-1470): n_trials
+ * independent trial_no_stdp_fixedSpread trials (:12747-13117), trial k drawing the noise
+ * streams of trial index first_trial + k, all in one batched run. */
+ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials);
+
+/* Per-instance spike statistics of the last batch: count and first step per neuron,
+ * arrays [n_trials][n].  which: 0 somatic (HVC-RA), 1 dendritic (HVC-RA), 2 HVC-I. */
+ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* count, int32_t* first_step);
+/* Every spike of one instance of the last batch, sorted by (neuron, step); step k is at
+ * time ug_step_time(k).  Replaces the spikes_in_trial_* arrays (NetworkGrowthSimulator.h). */
+ug_status ug_get_spikes(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t which, int32_t* neuron,
+                        int32_t* step, int64_t capacity, int64_t* n_out);
+/* Neuron state of one instance after the last batch: which 0 -> [n_ra][10]
+ * (Vs Vd n h l r c Ca Gexc_d Ginh_d), 1 -> [n_i][7] (V n m h w Gexc Ginh). */
+ug_status ug_get_neuron_state(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t which, double* out);
+/* internal_time after integration step `step` (NetworkGrowthSimulator.cpp:8925). */
+ug_status ug_step_time(ug_ctx* ctx, int32_t net_id, int32_t step, double* t);
+/* Number of kernels this context launched so far (graph replays count their nodes). */
+ug_status ug_launch_count(ug_ctx* ctx, int64_t* n);
+
+/* No counterpart in the reference (measurement support): measured throughput of the
+ * SFU (ex2/rcp approximations, operations per second) and of FP32 FMA on `device`,
+ * the denominators of the integrators' roofline. */
+ug_status ug_calibrate_pipes(int32_t device, double* mufu_ops_per_s, double* fma_ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,321 @@
+"""ORACLE / TEST INFRASTRUCTURE ONLY.
+
+ctypes wrapper of the CPU restatement (``ug_oracle.cpp``) and, where it was
+built, of the reference's own neuron classes (``_ref/libref.so``).  Only the
+tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import
+this module; the product package never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libref.so")
+
+RA_FIELDS = ("Vs", "Vd", "n", "h", "l", "r", "c", "Ca", "Gexc_d", "Ginh_d")
+I_FIELDS = ("V", "n", "m", "h", "w", "Gexc", "Ginh")
+
+
+class SynapticParams(C.Structure):
+    _fields_ = [("Nss", C.c_int32), ("_pad", C.c_int32)] + [
+        (n, C.c_double)
+        for n in ("A_P", "A_D", "T_0", "T_P", "T_D", "TAU_P", "TAU_D", "BETA", "BETA_SUPERSYNAPSE",
+                  "ACTIVATION_THRESHOLD", "SUPERSYNAPSE_THRESHOLD", "WEIGHT_MAX")
+    ]
+
+
+class MaturationParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("E_REST_MATURE", "E_REST_IMMATURE", "GCA_MATURE", "GCA_IMMATURE",
+                                          "DEATH_RATE_THRESHOLD")] + [("RATE_WINDOW_LONG", C.c_int32),
+                                                                      ("_pad", C.c_int32)]
+
+
+class NoiseParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("white_noise_mean_soma", "white_noise_std_soma",
+                                          "white_noise_mean_dend", "white_noise_std_dend")]
+
+
+class ConnectionParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("Gei_max", "Gie_max", "delay_constant", "A_RA2I", "SIGMA_RA2I",
+                                          "B_I2RA", "SIGMA_I2RA", "model_interneuron_distance")]
+
+
+def build(force: bool = False) -> str:
+    """Compile liboracle.so (and _ref/libref.so where the reference tree exists)."""
+    if force or not os.path.exists(LIB_PATH):
+        subprocess.run(["make", "-s", "all"], cwd=HERE, check=True)
+    return LIB_PATH
+
+
+def build_ref(ref_dir: str = "/root/reference/c++") -> str | None:
+    if not os.path.isdir(ref_dir):
+        return None
+    subprocess.run(["make", "-s", "ref", f"REF_DIR={ref_dir}"], cwd=HERE, check=True)
+    return REF_PATH
+
+
+_P = C.POINTER
+_i32p = _P(C.c_int32)
+_f64p = _P(C.c_double)
+_u8p = _P(C.c_uint8)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        L.ugo_new.restype = C.c_void_p
+        L.ugo_new.argtypes = [C.c_int32, C.c_int32]
+        L.ugo_free.argtypes = [C.c_void_p]
+        L.ugo_set_params.argtypes = [C.c_void_p, _P(SynapticParams), _P(MaturationParams), _P(NoiseParams),
+                                     _P(ConnectionParams)]
+        L.ugo_set_seed.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]
+        L.ugo_set_num_steps.argtypes = [C.c_void_p, C.c_int32]
+        for f in (L.ugo_set_ra2i, L.ugo_set_i2ra):
+            f.argtypes = [C.c_void_p, _i32p, _i32p, _f64p, _f64p, _f64p]
+        L.ugo_set_rara.argtypes = [C.c_void_p, _f64p, _f64p, _f64p]
+        L.ugo_set_synapse_lists.argtypes = [C.c_void_p, _i32p, _i32p, _i32p, _i32p]
+        L.ugo_set_neuron_props.argtypes = [C.c_void_p, _f64p, _f64p, _i32p, _f64p, _i32p, _i32p]
+        L.ugo_set_training.argtypes = [C.c_void_p, C.c_int32, _i32p, _f64p]
+        L.ugo_set_coordinates.argtypes = [C.c_void_p, _f64p, _f64p]
+        L.ugo_set_activity_history.argtypes = [C.c_void_p, _i32p]
+        L.ugo_set_trace.argtypes = [C.c_void_p, C.c_int32, _i32p, C.c_int32, _i32p]
+        L.ugo_get_trace.restype = C.c_int64
+        L.ugo_get_trace.argtypes = [C.c_void_p, C.c_int32, _f64p, C.c_int64]
+        L.ugo_set_delivery_log.argtypes = [C.c_void_p, C.c_int32]
+        L.ugo_get_delivery_log.restype = C.c_int64
+        L.ugo_get_delivery_log.argtypes = [C.c_void_p, _i32p, C.c_int64]
+        L.ugo_run_trial.restype = C.c_int32
+        L.ugo_run_trial.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]
+        L.ugo_after_growth_trial.restype = C.c_int32
+        L.ugo_after_growth_trial.argtypes = [C.c_void_p, C.c_uint32]
+        L.ugo_get_spikes.restype = C.c_int64
+        L.ugo_get_spikes.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, C.c_int64]
+        L.ugo_mean_injection_time.restype = C.c_double
+        L.ugo_mean_injection_time.argtypes = [C.c_void_p]
+        L.ugo_step_time.restype = C.c_double
+        L.ugo_step_time.argtypes = [C.c_void_p, C.c_int32]
+        L.ugo_get_weights.argtypes = [C.c_void_p, _f64p]
+        L.ugo_get_delays.argtypes = [C.c_void_p, _f64p]
+        L.ugo_get_list.restype = C.c_int64
+        L.ugo_get_list.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p]
+        L.ugo_get_neuron_props.argtypes = [C.c_void_p, _f64p, _f64p, _i32p, _f64p, _i32p, _i32p, _f64p]
+        L.ugo_get_connections.restype = C.c_int64
+        L.ugo_get_connections.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _f64p, _f64p]
+        L.ugo_get_coordinates.argtypes = [C.c_void_p, _f64p, _f64p]
+        L.ugo_get_replaced.restype = C.c_int64
+        L.ugo_get_replaced.argtypes = [C.c_void_p, _i32p, C.c_int64]
+        single_ra = [C.c_int32, C.c_double, C.c_double, _P(NoiseParams), C.c_uint64, C.c_uint32, C.c_uint32,
+                     _i32p, _f64p, _f64p, C.c_int32, _f64p, _u8p]
+        single_i = [C.c_int32, C.c_uint64, C.c_uint32, C.c_uint32, _i32p, _f64p, _f64p, C.c_int32, _f64p, _u8p]
+        L.ugo_ra_single.argtypes = single_ra
+        L.ugo_i_single.argtypes = single_i
+        L.ugo_philox.argtypes = [_P(C.c_uint32), _P(C.c_uint32), _P(C.c_uint32)]
+        L._single_ra = single_ra
+        L._single_i = single_i
+        _lib = L
+    return _lib
+
+
+_ref = None
+
+
+def ref_lib():
+    """The reference's own neuron classes, or None where they were not built."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            return None
+        R = C.CDLL(REF_PATH)
+        R.ref_ra_single.argtypes = lib()._single_ra
+        R.ref_i_single.argtypes = lib()._single_i
+        _ref = R
+    return _ref
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().ugo_philox(c, k, o)
+    return list(o)
+
+
+def _kicks(kicks):
+    kicks = sorted(kicks or [])
+    steps = np.array([k[0] for k in kicks], dtype=np.int32)
+    exc = np.array([k[1] for k in kicks], dtype=np.float64)
+    inh = np.array([k[2] for k in kicks], dtype=np.float64)
+    return steps, exc, inh
+
+
+def ra_single(n_steps, erest=-80.0, gca=55.0, noise=(0.0, 0.1, 0.0, 0.2), seed=1, trial=0, neuron=0,
+              kicks=None, use_ref=False):
+    """Step one HVC(RA) neuron n_steps times; kicks = [(step, exc, inh)] added before that step."""
+    L = ref_lib() if use_ref else lib()
+    if L is None:
+        raise RuntimeError("reference neuron classes not built")
+    fn = L.ref_ra_single if use_ref else L.ugo_ra_single
+    st, ex, ih = _kicks(kicks)
+    tr = np.zeros((n_steps, 10), dtype=np.float64)
+    fired = np.zeros((n_steps, 2), dtype=np.uint8)
+    npar = NoiseParams(*noise)
+    fn(n_steps, erest, gca, C.byref(npar), seed, trial, neuron, _ptr(st, _i32p), _ptr(ex, _f64p), _ptr(ih, _f64p),
+       len(st), _ptr(tr, _f64p), _ptr(fired, _u8p))
+    return tr, fired
+
+
+def i_single(n_steps, seed=1, trial=0, neuron=0, kicks=None, use_ref=False):
+    L = ref_lib() if use_ref else lib()
+    if L is None:
+        raise RuntimeError("reference neuron classes not built")
+    fn = L.ref_i_single if use_ref else L.ugo_i_single
+    st, ex, ih = _kicks(kicks)
+    tr = np.zeros((n_steps, 7), dtype=np.float64)
+    fired = np.zeros((n_steps,), dtype=np.uint8)
+    fn(n_steps, seed, trial, neuron, _ptr(st, _i32p), _ptr(ex, _f64p), _ptr(ih, _f64p), len(st),
+       _ptr(tr, _f64p), _ptr(fired, _u8p))
+    return tr, fired
+
+
+class OracleNet:
+    """One network held by the CPU restatement; mirrors the simulator's state."""
+
+    def __init__(self, net):
+        """net: a unsupervised_growth_gb300.network.Network-like object (numpy arrays)."""
+        self.L = lib()
+        self.n_ra, self.n_i = net.n_ra, net.n_i
+        self.h = self.L.ugo_new(self.n_ra, self.n_i)
+        self.window = int(net.mat["RATE_WINDOW_LONG"])
+        syn = SynapticParams(**net.syn)
+        mat = MaturationParams(**net.mat)
+        noi = NoiseParams(**net.noise)
+        con = ConnectionParams(**net.conn)
+        self.L.ugo_set_params(self.h, C.byref(syn), C.byref(mat), C.byref(noi), C.byref(con))
+        self.L.ugo_set_seed(self.h, int(net.seed), int(net.net_id))
+        self.L.ugo_set_num_steps(self.h, int(net.num_steps))
+        self.L.ugo_set_ra2i(self.h, *[_ptr(np.ascontiguousarray(a), t) for a, t in (
+            (net.ra2i_off, _i32p), (net.ra2i_tgt, _i32p), (net.ra2i_w, _f64p), (net.ra2i_d, _f64p),
+            (net.ra2i_len, _f64p))])
+        self.L.ugo_set_i2ra(self.h, *[_ptr(np.ascontiguousarray(a), t) for a, t in (
+            (net.i2ra_off, _i32p), (net.i2ra_tgt, _i32p), (net.i2ra_w, _f64p), (net.i2ra_d, _f64p),
+            (net.i2ra_len, _f64p))])
+        self.L.ugo_set_rara(self.h, _ptr(net.w_rara, _f64p), _ptr(net.d_rara, _f64p), _ptr(net.len_rara, _f64p))
+        self.L.ugo_set_synapse_lists(self.h, _ptr(net.active_off, _i32p), _ptr(net.active_tgt, _i32p),
+                                     _ptr(net.super_off, _i32p), _ptr(net.super_tgt, _i32p))
+        self.L.ugo_set_neuron_props(self.h, _ptr(net.rest_potential, _f64p), _ptr(net.gca, _f64p),
+                                    _ptr(net.mature, _i32p), _ptr(net.maturation_scale, _f64p),
+                                    _ptr(net.remodeled, _i32p), _ptr(net.trials_after_replacement, _i32p))
+        self.L.ugo_set_training(self.h, len(net.training), _ptr(net.training, _i32p),
+                                _ptr(net.training_spread, _f64p))
+        self.L.ugo_set_coordinates(self.h, _ptr(net.ra_xyz, _f64p), _ptr(net.i_xyz, _f64p))
+        self.L.ugo_set_activity_history(self.h, _ptr(net.activity_history, _i32p))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.ugo_free(self.h)
+            self.h = None
+
+    def set_trace(self, ra_ids=(), i_ids=()):
+        ra = np.asarray(ra_ids, dtype=np.int32)
+        ii = np.asarray(i_ids, dtype=np.int32)
+        self._tr = (len(ra), len(ii))
+        self.L.ugo_set_trace(self.h, len(ra), _ptr(ra, _i32p), len(ii), _ptr(ii, _i32p))
+
+    def trace(self):
+        n_ra, n_i = self._tr
+        out = []
+        for which, width, k in ((0, 10, n_ra), (1, 7, n_i)):
+            n = self.L.ugo_get_trace(self.h, which, None, 0)
+            buf = np.zeros(n, dtype=np.float64)
+            self.L.ugo_get_trace(self.h, which, _ptr(buf, _f64p), n)
+            out.append(buf.reshape(-1, k, width) if k else buf)
+        return out
+
+    def set_delivery_log(self, on=True):
+        self.L.ugo_set_delivery_log(self.h, 1 if on else 0)
+
+    def delivery_log(self):
+        n = self.L.ugo_get_delivery_log(self.h, None, 0)
+        out = np.zeros((n, 3), dtype=np.int32)
+        self.L.ugo_get_delivery_log(self.h, _ptr(out, _i32p), n)
+        return out
+
+    def run_trial(self, growth: bool, trial_index: int, training: bool = True) -> int:
+        return self.L.ugo_run_trial(self.h, 1 if growth else 0, 1 if training else 0, trial_index)
+
+    def after_growth_trial(self, trial_index: int) -> int:
+        return self.L.ugo_after_growth_trial(self.h, trial_index)
+
+    def spikes(self, which: int):
+        """which: 0 soma, 1 dendrite, 2 interneuron -> (neuron, step) arrays in detection order."""
+        n = self.L.ugo_get_spikes(self.h, which, None, None, 0)
+        nn = np.zeros(n, dtype=np.int32)
+        ss = np.zeros(n, dtype=np.int32)
+        self.L.ugo_get_spikes(self.h, which, _ptr(nn, _i32p), _ptr(ss, _i32p), n)
+        return nn, ss
+
+    def mean_injection_time(self):
+        return self.L.ugo_mean_injection_time(self.h)
+
+    def weights(self):
+        w = np.zeros((self.n_ra, self.n_ra), dtype=np.float64)
+        self.L.ugo_get_weights(self.h, _ptr(w, _f64p))
+        return w
+
+    def delays(self):
+        d = np.zeros((self.n_ra, self.n_ra), dtype=np.float64)
+        self.L.ugo_get_delays(self.h, _ptr(d, _f64p))
+        return d
+
+    def synapse_list(self, which: int):
+        """which 0 active, 1 super -> list of per-row ordered lists."""
+        n = self.L.ugo_get_list(self.h, which, None, None)
+        off = np.zeros(self.n_ra + 1, dtype=np.int32)
+        tgt = np.zeros(max(n, 1), dtype=np.int32)
+        self.L.ugo_get_list(self.h, which, _ptr(off, _i32p), _ptr(tgt, _i32p))
+        return [tgt[off[i]:off[i + 1]].tolist() for i in range(self.n_ra)]
+
+    def neuron_props(self):
+        N = self.n_ra
+        rest, gca, scale, frl = (np.zeros(N) for _ in range(4))
+        mature, remod, tar = (np.zeros(N, dtype=np.int32) for _ in range(3))
+        self.L.ugo_get_neuron_props(self.h, _ptr(rest, _f64p), _ptr(gca, _f64p), _ptr(mature, _i32p),
+                                    _ptr(scale, _f64p), _ptr(remod, _i32p), _ptr(tar, _i32p), _ptr(frl, _f64p))
+        return dict(rest_potential=rest, gca=gca, mature=mature, maturation_scale=scale, remodeled=remod,
+                    trials_after_replacement=tar, firing_rate_long=frl)
+
+    def connections(self, which: int):
+        n_src = self.n_ra if which == 0 else self.n_i
+        n = self.L.ugo_get_connections(self.h, which, None, None, None, None)
+        off = np.zeros(n_src + 1, dtype=np.int32)
+        tgt = np.zeros(max(n, 1), dtype=np.int32)
+        w = np.zeros(max(n, 1))
+        d = np.zeros(max(n, 1))
+        self.L.ugo_get_connections(self.h, which, _ptr(off, _i32p), _ptr(tgt, _i32p), _ptr(w, _f64p), _ptr(d, _f64p))
+        return off, tgt[:n], w[:n], d[:n]
+
+    def coordinates(self):
+        ra = np.zeros((self.n_ra, 3))
+        ii = np.zeros((self.n_i, 3))
+        self.L.ugo_get_coordinates(self.h, _ptr(ra, _f64p), _ptr(ii, _f64p))
+        return ra, ii
+
+    def replaced(self):
+        n = self.L.ugo_get_replaced(self.h, None, 0)
+        out = np.zeros(n, dtype=np.int32)
+        self.L.ugo_get_replaced(self.h, _ptr(out, _i32p), n)
+        return out

@@ -1,0 +1,245 @@
+"""ctypes binding of the C ABI in include/ugrowth.h.
+
+``Engine`` wraps one ``ug_ctx`` (one CUDA device); ``Engine.load_network``
+copies a ``network.Network`` to the device and returns a ``ResidentNetwork``
+whose methods map one-to-one onto the C entry points.  There is no CPU
+fallback: when ``libugrowth.so`` is missing or no GPU is present the calls
+raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .network import Network
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libugrowth.so")
+
+UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENUMERIC", 5: "UG_ETIMEOUT",
+             6: "UG_ECAPACITY", 7: "UG_ECUDA", 8: "UG_ENOTSUP"}
+
+# Every entry point of include/ugrowth.h, in declaration order.
+EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
+            "ug_free_network", "ug_run_test_trials", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
+            "ug_step_time", "ug_launch_count", "ug_calibrate_pipes"]
+
+
+class UGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{UG_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class SynapticParams(C.Structure):
+    _fields_ = [("Nss", C.c_int32), ("_pad", C.c_int32)] + [
+        (n, C.c_double)
+        for n in ("A_P", "A_D", "T_0", "T_P", "T_D", "TAU_P", "TAU_D", "BETA", "BETA_SUPERSYNAPSE",
+                  "ACTIVATION_THRESHOLD", "SUPERSYNAPSE_THRESHOLD", "WEIGHT_MAX")]
+
+
+class MaturationParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("E_REST_MATURE", "E_REST_IMMATURE", "GCA_MATURE", "GCA_IMMATURE",
+                                          "DEATH_RATE_THRESHOLD")] + [("RATE_WINDOW_LONG", C.c_int32),
+                                                                      ("_pad", C.c_int32)]
+
+
+class NoiseParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("white_noise_mean_soma", "white_noise_std_soma",
+                                          "white_noise_mean_dend", "white_noise_std_dend")]
+
+
+class ConnectionParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("Gei_max", "Gie_max", "delay_constant", "A_RA2I", "SIGMA_RA2I",
+                                          "B_I2RA", "SIGMA_I2RA", "model_interneuron_distance")]
+
+
+_i32p = C.POINTER(C.c_int32)
+_f64p = C.POINTER(C.c_double)
+
+
+class NetworkDesc(C.Structure):
+    _fields_ = [("n_ra", C.c_int32), ("n_i", C.c_int32), ("num_steps", C.c_int32), ("net_id", C.c_int32),
+                ("seed", C.c_uint64), ("syn", SynapticParams), ("mat", MaturationParams), ("noise", NoiseParams),
+                ("conn", ConnectionParams),
+                ("ra2i_off", _i32p), ("ra2i_tgt", _i32p), ("ra2i_w", _f64p), ("ra2i_d", _f64p), ("ra2i_len", _f64p),
+                ("i2ra_off", _i32p), ("i2ra_tgt", _i32p), ("i2ra_w", _f64p), ("i2ra_d", _f64p), ("i2ra_len", _f64p),
+                ("w_rara", _f64p), ("d_rara", _f64p), ("len_rara", _f64p),
+                ("active_off", _i32p), ("active_tgt", _i32p), ("super_off", _i32p), ("super_tgt", _i32p),
+                ("rest_potential", _f64p), ("gca", _f64p), ("mature", _i32p), ("maturation_scale", _f64p),
+                ("remodeled", _i32p), ("trials_after_replacement", _i32p), ("activity_history", _i32p),
+                ("n_tr", C.c_int32), ("training", _i32p), ("training_spread", _f64p),
+                ("ra_xyz", _f64p), ("i_xyz", _f64p)]
+
+
+class RuntimeOpts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("spike_capacity_per_neuron", C.c_int32),
+                ("use_graphs", C.c_int32)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libugrowth.so; raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with `python -m unsupervised_growth_gb300.build`")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.ug_last_error.restype = C.c_char_p
+    L.ug_create.argtypes = [C.POINTER(vp), C.POINTER(RuntimeOpts)]
+    L.ug_destroy.argtypes = [vp]
+    L.ug_destroy.restype = None
+    L.ug_set_stream.argtypes = [vp, vp]
+    L.ug_synchronize.argtypes = [vp]
+    L.ug_load_network.argtypes = [vp, C.POINTER(NetworkDesc), _i32p]
+    L.ug_free_network.argtypes = [vp, C.c_int32]
+    L.ug_run_test_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32]
+    L.ug_get_trial_stats.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p]
+    L.ug_get_spikes.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.POINTER(C.c_int64)]
+    L.ug_get_neuron_state.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _f64p]
+    L.ug_step_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p]
+    L.ug_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    for name in EXPORTED:
+        if name not in ("ug_last_error", "ug_destroy"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != 0:
+        raise UGError(status, load_library().ug_last_error().decode())
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class ResidentNetwork:
+    """A network resident in device memory."""
+
+    def __init__(self, engine: "Engine", net: Network, net_id: int):
+        self.engine, self.net, self.id = engine, net, net_id
+        self.n_ra, self.n_i = net.n_ra, net.n_i
+        self.batch = 0
+
+    def run_test_trials(self, first_trial: int, n_trials: int):
+        """n_trials independent test trials (trial_no_stdp_fixedSpread), noise streams first_trial + k."""
+        _check(self.engine.L.ug_run_test_trials(self.engine.ctx, self.id, first_trial, n_trials))
+        self.batch = n_trials
+
+    def trial_stats(self, which: int):
+        """(count, first_step) arrays [n_trials][n]; which 0 soma, 1 dendrite, 2 interneuron."""
+        n = self.n_i if which == 2 else self.n_ra
+        cnt = np.zeros((self.batch, n), dtype=np.int32)
+        first = np.zeros((self.batch, n), dtype=np.int32)
+        _check(self.engine.L.ug_get_trial_stats(self.engine.ctx, self.id, which, _p(cnt, _i32p), _p(first, _i32p)))
+        return cnt, first
+
+    def spikes(self, instance: int, which: int):
+        """(neuron, step) arrays sorted by neuron then step."""
+        n = C.c_int64(0)
+        _check(self.engine.L.ug_get_spikes(self.engine.ctx, self.id, instance, which, None, None, 0, C.byref(n)))
+        nn = np.zeros(n.value, dtype=np.int32)
+        ss = np.zeros(n.value, dtype=np.int32)
+        _check(self.engine.L.ug_get_spikes(self.engine.ctx, self.id, instance, which, _p(nn, _i32p), _p(ss, _i32p),
+                                           n.value, C.byref(n)))
+        return nn, ss
+
+    def neuron_state(self, instance: int, which: int):
+        shape = (self.n_ra, 10) if which == 0 else (self.n_i, 7)
+        out = np.zeros(shape, dtype=np.float64)
+        _check(self.engine.L.ug_get_neuron_state(self.engine.ctx, self.id, instance, which, _p(out, _f64p)))
+        return out
+
+    def step_time(self, step: int) -> float:
+        t = C.c_double(0)
+        _check(self.engine.L.ug_step_time(self.engine.ctx, self.id, step, C.byref(t)))
+        return t.value
+
+    def free(self):
+        if self.id is not None:
+            _check(self.engine.L.ug_free_network(self.engine.ctx, self.id))
+            self.id = None
+
+
+class Engine:
+    def __init__(self, precision: int = 32, device: int = 0, spike_capacity_per_neuron: int = 16,
+                 use_graphs: bool = True):
+        self.L = load_library()
+        self.ctx = C.c_void_p()
+        opts = RuntimeOpts(precision, device, spike_capacity_per_neuron, 1 if use_graphs else 0)
+        _check(self.L.ug_create(C.byref(self.ctx), C.byref(opts)))
+        self.precision = precision
+        self._keep = []
+
+    def close(self):
+        if self.ctx:
+            self.L.ug_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        _check(self.L.ug_set_stream(self.ctx, C.c_void_p(stream_handle) if stream_handle else None))
+
+    def synchronize(self):
+        _check(self.L.ug_synchronize(self.ctx))
+
+    def launch_count(self) -> int:
+        n = C.c_int64(0)
+        _check(self.L.ug_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
+    def load_network(self, net: Network) -> ResidentNetwork:
+        d, keep = make_desc(net)
+        nid = C.c_int32(-1)
+        _check(self.L.ug_load_network(self.ctx, C.byref(d), C.byref(nid)))
+        return ResidentNetwork(self, net, nid.value)
+
+
+def calibrate_pipes(device: int = 0):
+    """Measured (MUFU ops/s, FP32 FMA ops/s) of the device."""
+    L = load_library()
+    a, b = C.c_double(0), C.c_double(0)
+    _check(L.ug_calibrate_pipes(device, C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
+def make_desc(net: Network):
+    """Fills a ug_network_desc that points into the network's arrays."""
+    keep = []
+
+    def arr(a, dtype):
+        if a is None:
+            return None
+        x = np.ascontiguousarray(a, dtype=dtype)
+        keep.append(x)
+        return x.ctypes.data_as(_i32p if dtype == np.int32 else _f64p)
+
+    d = NetworkDesc()
+    d.n_ra, d.n_i, d.num_steps, d.net_id, d.seed = net.n_ra, net.n_i, net.num_steps, net.net_id, net.seed
+    d.syn = SynapticParams(**net.syn)
+    d.mat = MaturationParams(**net.mat)
+    d.noise = NoiseParams(**net.noise)
+    d.conn = ConnectionParams(**net.conn)
+    for f in ("ra2i_off", "ra2i_tgt", "i2ra_off", "i2ra_tgt", "active_off", "active_tgt", "super_off", "super_tgt",
+              "mature", "remodeled", "trials_after_replacement", "activity_history", "training"):
+        setattr(d, f, arr(getattr(net, f), np.int32))
+    for f in ("ra2i_w", "ra2i_d", "ra2i_len", "i2ra_w", "i2ra_d", "i2ra_len", "w_rara", "d_rara", "len_rara",
+              "rest_potential", "gca", "maturation_scale", "training_spread", "ra_xyz", "i_xyz"):
+        setattr(d, f, arr(getattr(net, f), np.float64))
+    d.n_tr = len(net.training)
+    d._keep = keep
+    return d, keep
