@@ -33,9 +33,13 @@ N_RA, N_I, GROUPS, GROUP, WEIGHT = 2000, 550, 20, 100, 500.0
 NUM_STEPS = 25000
 BATCH = 1024
 SEED = 3
-# Algorithmic SFU work per neuron-step of the single-precision integrators,
-# counted from ug_neuron.cuh: RA 4 stages x (8 ex2 + 7 rcp); I 12 stages x (7 ex2 + 4 rcp).
-MUFU_RA, MUFU_I = 60, 132
+# Work per neuron-step of the single-precision integrators, counted from their
+# source (csrc/ug_ra_f32x2.cuh, csrc/ug_i_f32.cuh): FP32 lane operations (a packed
+# f32x2 operation counts 2) and SFU operations (ex2, rcp).
+#   RA: 4 stages x 90 packed ops + 128 packed ops of stage sums  = 488 FP32 ops; 4 x (8 ex2 + 2 rcp) = 40 SFU
+#   I : 12 stages x 63 ops + 376 ops of the DP8 tableau sums      = 1132 FP32 ops; 12 x (4 ex2 + 1 rcp) = 60 SFU
+FP32_RA, FP32_I = 488, 1132
+MUFU_RA, MUFU_I = 40, 60
 CPU_SAMPLE_STEPS = 6000   # first 120 ms of a trial (includes the training kick at 100 ms)
 
 
@@ -124,9 +128,37 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- GPU arm
+def _fp64_plain(net, device, trial, rn32):
+    """Times one trial of the plain double-precision path (no batching, no graph)
+    and compares the single build's spikes of the same trial with it."""
+    from tests.helpers import match_within, sorted_spikes
+    from unsupervised_growth_gb300.engine import Engine
+    eng64 = Engine(precision=64, device=device, use_graphs=False)
+    rn64 = eng64.load_network(net)
+    rn64.run_test_trials(trial, 1)
+    eng64.synchronize()
+    t0 = time.perf_counter()
+    rn64.run_test_trials(trial, 1)
+    eng64.synchronize()
+    fp64_s = time.perf_counter() - t0
+    rn32.run_test_trials(trial, 1)
+    acc = {}
+    for w, name in ((0, "soma"), (1, "dend"), (2, "interneuron")):
+        a = sorted_spikes(*rn32.spikes(0, w))
+        b = sorted_spikes(*rn64.spikes(0, w))
+        frac, worst = match_within(a, b, 1)
+        acc[name] = {"spikes_fp32": int(len(a)), "spikes_fp64": int(len(b)), "matched_within_1_step": frac,
+                     "max_step_error": worst}
+    rn64.free()
+    eng64.close()
+    return fp64_s, acc
+
+
 def run_ours(args, rank, world, local_rank):
-    import numpy as np
     import torch
+
+    global BATCH
+    BATCH = args.batch
 
     from unsupervised_growth_gb300 import build as B
     from unsupervised_growth_gb300.engine import Engine, calibrate_pipes
@@ -139,7 +171,7 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl")
 
     net = make_network()
-    eng = Engine(precision=32, device=local_rank, spike_capacity_per_neuron=16, use_graphs=True)
+    eng = Engine(precision=32, device=local_rank, spike_capacity_per_neuron=16, use_graphs=not args.no_graphs)
     # a dedicated stream: the engine's kernels and the timing events share it
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
@@ -194,34 +226,30 @@ def run_ours(args, rank, world, local_rank):
         value = trials / (total_ms / 1e3)
         e2e_value = BATCH * args.steps * world / max(sum(e2e_s), 1e-9)
         mufu_peak, fma_peak = calibrate_pipes(local_rank)
-        n_launch_interval = NUM_STEPS - 1
-        avg_interval = 24999 / 2000.0
-        mufu_per_launch = BATCH * (N_RA * MUFU_RA + N_I * MUFU_I) * avg_interval
-        avg_launch_ms = (sum(step_ms) / args.steps) / (2000 + 1)
-        achieved = mufu_per_launch / (avg_launch_ms * 1e-3)
+        # per-kernel device time: one more batch with every launch bracketed by events
+        eng.set_kernel_timing(True)
+        rn.run_test_trials(first, BATCH)
+        kt = {k: eng.kernel_timing(k) for k in ("k_interval_ra", "k_interval_i", "k_trial_init")}
+        eng.set_kernel_timing(False)
+        avg_steps = (NUM_STEPS - 1) / 2000.0   # integration steps per interval launch
+        neuron_steps = {"k_interval_ra": BATCH * N_RA * avg_steps, "k_interval_i": BATCH * N_I * avg_steps}
+        fp32_ops = {"k_interval_ra": FP32_RA, "k_interval_i": FP32_I}
+        sfu_ops = {"k_interval_ra": MUFU_RA, "k_interval_i": MUFU_I}
+        kernels = {}
+        total_kernel_ms = max(sum(v[0] for v in kt.values()), 1e-9)
+        for k, ns in neuron_steps.items():
+            ms, cnt = kt[k]
+            avg_ms = ms / max(cnt, 1)
+            sec = max(avg_ms, 1e-9) * 1e-3
+            kernels[k] = {"launches": cnt, "avg_launch_ms": avg_ms, "share": ms / total_kernel_ms,
+                          "fp32_ops_per_launch": ns * fp32_ops[k], "fp32_frac": ns * fp32_ops[k] / sec / fma_peak,
+                          "sfu_ops_per_launch": ns * sfu_ops[k], "sfu_frac": ns * sfu_ops[k] / sec / mufu_peak}
+        dom = max(neuron_steps, key=lambda k: kt[k][0])
+        per_launch = kernels[dom]["fp32_ops_per_launch"]
+        achieved = per_launch / (kernels[dom]["avg_launch_ms"] * 1e-3)
 
         # plain double-precision GPU path: one trial per run, no batching, no graph
-        eng64 = Engine(precision=64, device=local_rank, use_graphs=False)
-        rn64 = eng64.load_network(net)
-        rn64.run_test_trials(first, 1)
-        eng64.synchronize()
-        t0 = time.perf_counter()
-        rn64.run_test_trials(first, 1)
-        eng64.synchronize()
-        fp64_s = time.perf_counter() - t0
-        # accuracy of the single build against the double build on the same trial
-        from tests.helpers import match_within, sorted_spikes
-        rn.run_test_trials(first, 1)
-        acc = {}
-        for w, name in ((0, "soma"), (1, "dend"), (2, "interneuron")):
-            a = sorted_spikes(*rn.spikes(0, w))
-            b = sorted_spikes(*rn64.spikes(0, w))
-            frac, worst = match_within(a, b, 1)
-            acc[name] = {"spikes_fp32": int(len(a)), "spikes_fp64": int(len(b)), "matched_within_1_step": frac,
-                         "max_step_error": worst}
-        rn64.free()
-        eng64.close()
-
+        fp64 = None if args.skip_fp64 else _fp64_plain(net, local_rank, first, rn)
         cores = min(os.cpu_count() or 1, 16)
         cpu_rate, cpu_times = cpu_sample(cores) if not args.skip_cpu else (None, [])
         result = {
@@ -233,17 +261,21 @@ def run_ours(args, rank, world, local_rank):
             "neuron_steps_per_s": value * (N_RA + N_I) * (NUM_STEPS - 1),
             "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": mufu_peak / 1e9, "unit": "GMUFU/s",
-                         "frac": achieved / mufu_peak, "traffic": None,
-                         "kernel": "k_interval<float>",
-                         "peak_source": "ex2.approx+rcp.approx throughput loop (ug_calibrate_pipes), this run",
-                         "fma_peak_gops": fma_peak / 1e9,
-                         "algorithmic_per_launch": f"{mufu_per_launch:.4g} MUFU ops"},
-            "fp64_plain_gpu": {"trials_per_s": 1.0 / fp64_s, "speedup_of_value": value * fp64_s},
-            "accuracy_vs_fp64": acc,
+            "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fma_peak / 1e12, "unit": "T FP32 ops/s",
+                         "frac": achieved / fma_peak, "traffic": None, "kernel": dom,
+                         "peak_source": "FP32 FMA throughput loop (ug_calibrate_pipes), measured in this run; "
+                                        "SFU peak (ex2+rcp loop) also measured",
+                         "sfu_peak_gops": mufu_peak / 1e9, "kernels": kernels,
+                         "algorithmic_per_launch": f"{per_launch:.4g} FP32 ops (RA {FP32_RA}, I {FP32_I} per "
+                                                   f"neuron-step x neurons x {avg_steps:.4f} steps x {BATCH} trials)"},
             "soma_spikes_per_trial": spikes_per_trial,
             "clocks": clk.summary(),
         }
+        if fp64 is not None:
+            fp64_s, acc = fp64
+            result["fp64_plain_gpu"] = {"trials_per_s": 1.0 / fp64_s, "speedup_of_value": value * fp64_s,
+                                        "how": "one trial per run, no batching, no graph, double precision"}
+            result["accuracy_vs_fp64"] = acc
         if cpu_rate is not None:
             result["cpu_baseline"] = {"value": cpu_rate, "unit": "trials/s", "cores": cores, "kind": "port",
                                       "sample": f"oracle/ (double-precision CPU restatement) on {cores} processes, "
@@ -284,7 +316,10 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--batch", type=int, default=BATCH, help="test trials per step (profiling runs use fewer)")
+    ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
+    ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
+    ap.add_argument("--skip-fp64", action="store_true", help="do not time the plain double-precision GPU path")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))

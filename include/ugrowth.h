@@ -132,6 +132,12 @@ ug_status ug_get_neuron_state(ug_ctx* ctx, int32_t net_id, int32_t instance, int
 ug_status ug_step_time(ug_ctx* ctx, int32_t net_id, int32_t step, double* t);
 /* Number of kernels this context launched so far (graph replays count their nodes). */
 ug_status ug_launch_count(ug_ctx* ctx, int64_t* n);
+/* No counterpart in the reference (measurement support).  While enabled, batches are
+ * launched without graphs, one kernel at a time, each bracketed by CUDA events; enabling
+ * or disabling clears the totals.  ug_get_kernel_timing returns the summed device time and
+ * launch count of one kernel: "k_trial_init", "k_interval_ra" or "k_interval_i". */
+ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled);
+ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches);
 
 /* No counterpart in the reference (measurement support): measured throughput of the
  * SFU (ex2/rcp approximations, operations per second) and of FP32 FMA on `device`,

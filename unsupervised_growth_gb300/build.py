@@ -15,8 +15,10 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
-OUT_DIR = os.path.join(HERE, "_lib")
+OUT_DIR = os.environ.get("UG_BUILD_DIR", os.path.join(HERE, "_lib"))
 LIB = os.path.join(OUT_DIR, "libugrowth.so")
+# extra nvcc flags, e.g. -DUG_RA_MIN_BLOCKS=4 to build a tuning variant into UG_BUILD_DIR
+EXTRA = os.environ.get("UG_NVCC_EXTRA", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
@@ -51,7 +53,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     def compile_unit(unit):
         src, extra = unit
         obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
+        cmd = [nvcc()] + ARCH + COMMON + EXTRA + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

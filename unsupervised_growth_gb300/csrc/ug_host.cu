@@ -128,7 +128,7 @@ struct NetHost {
 class NetBase {
 public:
     virtual ~NetBase() = default;
-    virtual ug_status run_test_trials(uint32_t first_trial, int n_trials, cudaStream_t st, bool graphs,
+    virtual ug_status run_test_trials(uint32_t first_trial, int n_trials, const ug::LaunchCtx& lc, bool graphs,
                                       int64_t* launches) = 0;
     virtual ug_status stats(int which, int32_t* count, int32_t* first, cudaStream_t st) = 0;
     virtual ug_status spikes(int instance, int which, int32_t* neuron, int32_t* step, int64_t cap, int64_t* n,
@@ -172,7 +172,7 @@ template <class R>
 class NetImpl : public NetBase {
 public:
     ug_status init(const ug_network_desc* d, int spike_cap_per_neuron, cudaStream_t st);
-    ug_status run_test_trials(uint32_t first_trial, int n_trials, cudaStream_t st, bool graphs,
+    ug_status run_test_trials(uint32_t first_trial, int n_trials, const ug::LaunchCtx& lc, bool graphs,
                               int64_t* launches) override;
     ug_status stats(int which, int32_t* count, int32_t* first, cudaStream_t st) override;
     ug_status spikes(int instance, int which, int32_t* neuron, int32_t* step, int64_t cap, int64_t* n,
@@ -186,7 +186,7 @@ public:
 private:
     ug_status ensure_batch(int B);
     ug_status check_error(cudaStream_t st);
-    ug_status issue_batch(cudaStream_t st, int64_t* launches);
+    ug_status issue_batch(const ug::LaunchCtx& lc, int64_t* launches);
 
     ug::NetDev<R> nd_{};
     ug::BatchDev<R> bd_{};
@@ -197,8 +197,8 @@ private:
     int B_cap_ = 0;        // allocated instances
     DevMem dT_, dSyncidx_, dRaDecay_, dIDecay_, dErest_, dGCa_, dSpread_, dTraining_;
     CsrDev ra2i_, i2ra_, rara_;
-    DevMem ra_[10], ra_flags_, ra_nsoma_, ra_ndend_, ra_first_soma_, ra_first_dend_;
-    DevMem iv_[7], i_noise_, i_word_, i_flag_, i_nspk_, i_first_;
+    DevMem ra_[10], ra_flags_, kick_step_, ra_nsoma_, ra_ndend_, ra_first_soma_, ra_first_dend_;
+    DevMem iv_[7], i_noise_, i_noise_step_, i_events_, i_ev_idx_, i_word_, i_flag_, i_nspk_, i_first_;
     DevMem ring_ra_exc_, ring_ra_inh_, ring_i_exc_, spk_buf_, spk_count_, error_, trial_, mean_inj_;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_B_ = -1;
@@ -350,9 +350,14 @@ ug_status NetImpl<R>::ensure_batch(int B)
     if (B <= B_cap_) return UG_OK;
     const size_t nra = (size_t)B * h.n_ra, ni = (size_t)B * h.n_i;
     for (int k = 0; k < 10; ++k) UG_TRY(ra_[k].alloc(nra * sizeof(R)));
-    for (DevMem* m : {&ra_flags_, &ra_nsoma_, &ra_ndend_, &ra_first_soma_, &ra_first_dend_}) UG_TRY(m->alloc(nra * sizeof(int)));
+    for (DevMem* m : {&ra_flags_, &kick_step_, &ra_nsoma_, &ra_ndend_, &ra_first_soma_, &ra_first_dend_}) UG_TRY(m->alloc(nra * sizeof(int)));
     for (int k = 0; k < 7; ++k) UG_TRY(iv_[k].alloc(ni * sizeof(R)));
     UG_TRY(i_noise_.alloc(2 * ni * sizeof(double)));
+    UG_TRY(i_noise_step_.alloc(2 * ni * sizeof(int)));
+    // noise events per interneuron channel and trial: 250 Hz on average (HHI_buffer.cpp:37)
+    const int ev_cap = sizeof(R) == 4 ? (int)(h.num_steps * 0.02 * 0.25 * 2.0) + 64 : 1;
+    UG_TRY(i_events_.alloc(2 * ni * (size_t)ev_cap * sizeof(int2)));
+    UG_TRY(i_ev_idx_.alloc(2 * ni * sizeof(int)));
     for (DevMem* m : {&i_word_, &i_flag_, &i_nspk_, &i_first_}) UG_TRY(m->alloc(ni * sizeof(int)));
     UG_TRY(ring_ra_exc_.alloc((size_t)ring * nra * sizeof(long long)));
     UG_TRY(ring_ra_inh_.alloc((size_t)ring * nra * sizeof(long long)));
@@ -370,10 +375,11 @@ ug_status NetImpl<R>::ensure_batch(int B)
     }
     ug::BatchDev<R>& b = bd_;
     for (int k = 0; k < 10; ++k) b.ra[k] = ra_[k].as<R>();
-    b.ra_flags = ra_flags_.as<int>(); b.ra_nsoma = ra_nsoma_.as<int>(); b.ra_ndend = ra_ndend_.as<int>();
+    b.ra_flags = ra_flags_.as<int>(); b.kick_step = kick_step_.as<int>(); b.ra_nsoma = ra_nsoma_.as<int>(); b.ra_ndend = ra_ndend_.as<int>();
     b.ra_first_soma = ra_first_soma_.as<int>(); b.ra_first_dend = ra_first_dend_.as<int>();
     for (int k = 0; k < 7; ++k) b.iv[k] = iv_[k].as<R>();
-    b.i_noise = i_noise_.as<double>(); b.i_word = i_word_.as<uint32_t>(); b.i_flag = i_flag_.as<int>();
+    b.i_noise = i_noise_.as<double>(); b.i_noise_step = i_noise_step_.as<int>();
+    b.i_events = i_events_.as<int2>(); b.i_ev_idx = i_ev_idx_.as<int>(); b.ev_cap = ev_cap; b.i_word = i_word_.as<uint32_t>(); b.i_flag = i_flag_.as<int>();
     b.i_nspk = i_nspk_.as<int>(); b.i_first = i_first_.as<int>();
     b.ring_ra_exc = ring_ra_exc_.as<long long>(); b.ring_ra_inh = ring_ra_inh_.as<long long>();
     b.ring_i_exc = ring_i_exc_.as<long long>();
@@ -385,24 +391,26 @@ ug_status NetImpl<R>::ensure_batch(int B)
 }
 
 template <class R>
-ug_status NetImpl<R>::issue_batch(cudaStream_t st, int64_t* launches)
+ug_status NetImpl<R>::issue_batch(const ug::LaunchCtx& lc, int64_t* launches)
 {
-    UG_CUDA(ug::launch_trial_init<R>(nd_, bd_, st));
+    UG_CUDA(ug::launch_trial_init<R>(nd_, bd_, lc));
     const int Q = (int)sync_steps.size();
     for (int q = 0; q < Q; ++q) {
         const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
-        UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, st));
+        UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, lc));
     }
     // The last sync (forced at t == num_steps - 1) also raises the conductances
     // (NetworkGrowthSimulator.cpp:9291); an empty interval applies its kicks.
-    UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, st));
-    if (launches) *launches += Q + 2;
+    UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
+    if (launches) *launches += 2 * (Q + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
     return UG_OK;
 }
 
 template <class R>
-ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, cudaStream_t st, bool graphs, int64_t* launches)
+ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const ug::LaunchCtx& lc, bool graphs,
+                                      int64_t* launches)
 {
+    cudaStream_t st = lc.main;
     if (n_trials <= 0 || n_trials > 65535) return fail(UG_EINVAL, "n_trials must be in [1, 65535]");
     UG_TRY(ensure_batch(n_trials));
     bd_.B = n_trials;
@@ -414,7 +422,7 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, cudaSt
     for (int k = 0; k < n_trials; ++k) tr[k] = first_trial + (uint32_t)k;
     UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), tr.data(), tr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), mi.data(), mi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    if (!graphs) return issue_batch(st, launches);
+    if (!graphs || lc.timer) return issue_batch(lc, launches);
     if (!graph_exec_ || graph_B_ != n_trials) {
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
@@ -425,7 +433,9 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, cudaSt
         cudaGraph_t g;
         UG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
         int64_t dummy = 0;
-        ug_status s = issue_batch(cap, &dummy);
+        ug::LaunchCtx clc = lc;
+        clc.main = cap;
+        ug_status s = issue_batch(clc, &dummy);
         cudaError_t e = cudaStreamEndCapture(cap, &g);
         cudaStreamDestroy(cap);
         if (s != UG_OK) return s;
@@ -436,7 +446,7 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, cudaSt
         graph_B_ = n_trials;
     }
     UG_CUDA(cudaGraphLaunch(graph_exec_, st));
-    if (launches) *launches += (int64_t)sync_steps.size() + 2;
+    if (launches) *launches += 2 * ((int64_t)sync_steps.size() + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
     return UG_OK;
 }
 
@@ -516,6 +526,19 @@ struct ug_ctx {
     bool graphs = true;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    ug::KernelTimer timer;
+    ug::LaunchCtx launch_ctx()
+    {
+        ug::LaunchCtx lc;
+        lc.main = stream;
+        lc.side = side;
+        lc.fork = fork;
+        lc.join = join;
+        lc.timer = timer.enabled ? &timer : nullptr;
+        return lc;
+    }
     int64_t launches = 0;
     int next_id = 0;
     std::map<int, std::unique_ptr<NetBase>> nets;
@@ -555,6 +578,9 @@ ug_status ug_create(ug_ctx** out, const ug_runtime_opts* opts)
     if (c->device < 0 || c->device >= ndev) return fail(UG_EINVAL, "no such CUDA device");
     UG_CUDA(cudaSetDevice(c->device));
     UG_CUDA(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking));
+    UG_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+    UG_CUDA(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
+    UG_CUDA(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
     c->stream = c->own;
     *out = c.release();
     return UG_OK;
@@ -565,7 +591,12 @@ void ug_destroy(ug_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(ctx->side);
     ctx->nets.clear();
+    ctx->timer.clear(true);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -621,7 +652,7 @@ ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, 
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaSetDevice(ctx->device));
-    return n->run_test_trials(first_trial, n_trials, ctx->stream, ctx->graphs, &ctx->launches);
+    return n->run_test_trials(first_trial, n_trials, ctx->launch_ctx(), ctx->graphs, &ctx->launches);
 }
 
 ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* count, int32_t* first_step)
@@ -655,6 +686,26 @@ ug_status ug_step_time(ug_ctx* ctx, int32_t net_id, int32_t step, double* t)
     UG_TRY(get_net(ctx, net_id, &n));
     if (step < 0 || step >= (int)n->T.size() || !t) return fail(UG_EINVAL, "step out of range");
     *t = n->T[step];
+    return UG_OK;
+}
+
+ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    UG_CUDA(cudaStreamSynchronize(ctx->stream));
+    UG_CUDA(ctx->timer.collect());
+    ctx->timer.clear(false);
+    ctx->timer.enabled = enabled != 0;
+    return UG_OK;
+}
+
+ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches)
+{
+    if (!ctx || !kernel || !total_ms || !launches) return fail(UG_EINVAL, "null argument");
+    UG_CUDA(ctx->timer.collect());
+    long long n = 0;
+    ctx->timer.totals(kernel, total_ms, &n);
+    *launches = n;
     return UG_OK;
 }
 

@@ -2,7 +2,7 @@
 #include "ug_kernels_inst.cuh"
 
 namespace ug {
-template cudaError_t launch_trial_init<float>(const NetDev<float>&, const BatchDev<float>&, cudaStream_t);
+template cudaError_t launch_trial_init<float>(const NetDev<float>&, const BatchDev<float>&, const LaunchCtx&);
 template cudaError_t launch_interval<float>(const NetDev<float>&, const BatchDev<float>&, int, int, int,
-                                            const RAStep<float>&, const IStep<float>&, cudaStream_t);
+                                            const RAStep<float>&, const IStep<float>&, const LaunchCtx&);
 }  // namespace ug

@@ -4,20 +4,95 @@
 
 namespace ug {
 
+#define UG_TIMED(lc, name, launch)                                      \
+    do {                                                                \
+        if ((lc).timer) {                                               \
+            cudaError_t e_ = (lc).timer->begin(name, (lc).main);        \
+            if (e_ != cudaSuccess) return e_;                           \
+        }                                                               \
+        launch;                                                         \
+        if ((lc).timer) {                                               \
+            cudaError_t e_ = (lc).timer->end((lc).main);                \
+            if (e_ != cudaSuccess) return e_;                           \
+        }                                                               \
+    } while (0)
+
+// Single build only: pre-draw the interneurons' noise events of the trial.
+inline void launch_noise_events(const NetDev<double>&, const BatchDev<double>&, const LaunchCtx&) {}
+inline void launch_noise_events(const NetDev<float>& n, const BatchDev<float>& b, const LaunchCtx& lc)
+{
+    if (n.n_i == 0) return;
+    if (lc.timer) lc.timer->begin("k_noise_events", lc.main);
+    k_noise_events<float><<<dim3((n.n_i + kBlock - 1) / kBlock, b.B), kBlock, 0, lc.main>>>(n, b);
+    if (lc.timer) lc.timer->end(lc.main);
+}
+
+inline void launch_i(const NetDev<double>& n, const BatchDev<double>& b, int q, int s0, int s1,
+                     const IStep<double>& ic, cudaStream_t st, const LaunchCtx& lc)
+{
+    if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
+    k_interval_i<double><<<dim3((n.n_i + kBlock - 1) / kBlock, b.B), kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    if (lc.timer) lc.timer->end(lc.main);
+}
+
+inline void launch_i(const NetDev<float>& n, const BatchDev<float>& b, int q, int s0, int s1, const IStep<float>& ic,
+                     cudaStream_t st, const LaunchCtx& lc)
+{
+    if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
+    k_interval_i_x<float><<<dim3((n.n_i + kBlock - 1) / kBlock, b.B), kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    if (lc.timer) lc.timer->end(lc.main);
+}
+
 template <class R>
-cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, cudaStream_t st)
+cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, const LaunchCtx& lc)
 {
     const dim3 grid((n.n_ra + kBlock - 1) / kBlock + (n.n_i + kBlock - 1) / kBlock, b.B);
-    k_trial_init<R><<<grid, kBlock, 0, st>>>(n, b);
+    UG_TIMED(lc, "k_trial_init", (k_trial_init<R><<<grid, kBlock, 0, lc.main>>>(n, b)));
+    launch_noise_events(n, b, lc);
     return cudaGetLastError();
+}
+
+// HVC(RA) interval kernel: the double build steps one neuron per thread, the
+// single build two neurons per thread with packed f32x2 arithmetic.
+inline void launch_ra(const NetDev<double>& n, const BatchDev<double>& b, int q, int s0, int s1,
+                      const RAStep<double>& rc, const LaunchCtx& lc)
+{
+    const dim3 g((n.n_ra + kBlock - 1) / kBlock, b.B);
+    if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
+    k_interval_ra<double><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    if (lc.timer) lc.timer->end(lc.main);
+}
+
+inline void launch_ra(const NetDev<float>& n, const BatchDev<float>& b, int q, int s0, int s1, const RAStep<float>& rc,
+                      const LaunchCtx& lc)
+{
+    const dim3 g(((n.n_ra + 1) / 2 + kBlock - 1) / kBlock, b.B);
+    if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
+    k_interval_ra_x2<float><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    if (lc.timer) lc.timer->end(lc.main);
 }
 
 template <class R>
 cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1, const RAStep<R>& rc,
-                            const IStep<R>& ic, cudaStream_t st)
+                            const IStep<R>& ic, const LaunchCtx& lc)
 {
-    const dim3 grid((n.n_ra + kBlock - 1) / kBlock + (n.n_i + kBlock - 1) / kBlock, b.B);
-    k_interval<R><<<grid, kBlock, 0, st>>>(n, b, q, s0, s1, rc, ic);
+    // Overlap the two kernels only when a batch is too small to fill the GPU on
+    // its own; large batches run them back to back so each SM executes one
+    // kernel's code at a time (the integrators do not fit the instruction cache together).
+    const bool fork = !lc.timer && lc.side && lc.side != lc.main && n.n_i > 0 && b.B < 16;
+    cudaStream_t si = fork ? lc.side : lc.main;
+    if (fork) {
+        cudaError_t e = cudaEventRecord(lc.fork, lc.main);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.side, lc.fork, 0);
+        if (e != cudaSuccess) return e;
+    }
+    launch_ra(n, b, q, s0, s1, rc, lc);
+    if (n.n_i > 0) launch_i(n, b, q, s0, s1, ic, si, lc);
+    if (fork) {
+        cudaError_t e = cudaEventRecord(lc.join, lc.side);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.main, lc.join, 0);
+        if (e != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 

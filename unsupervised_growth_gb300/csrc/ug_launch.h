@@ -3,15 +3,101 @@
 // contraction so it keeps the reference's rounding sequence).
 #pragma once
 #include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
 #include "ug_trial.cuh"
 
 namespace ug {
 
+// Per-kernel device time from CUDA events bracketing each launch (only for
+// launches that are not captured into a graph).
+class KernelTimer {
+public:
+    ~KernelTimer() { clear(true); }
+    bool enabled = false;
+    cudaError_t begin(const char* name, cudaStream_t st)
+    {
+        Pending p;
+        p.name = name;
+        cudaError_t e = take(&p.a);
+        if (e == cudaSuccess) e = take(&p.b);
+        if (e == cudaSuccess) e = cudaEventRecord(p.a, st);
+        pending_.push_back(p);
+        return e;
+    }
+    cudaError_t end(cudaStream_t st) { return cudaEventRecord(pending_.back().b, st); }
+    // Folds completed launches into the totals (synchronizes on their events).
+    cudaError_t collect()
+    {
+        for (Pending& p : pending_) {
+            cudaError_t e = cudaEventSynchronize(p.b);
+            if (e != cudaSuccess) return e;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, p.a, p.b);
+            Total& t = totals_[p.name];
+            t.ms += ms;
+            t.count += 1;
+            pool_.push_back(p.a);
+            pool_.push_back(p.b);
+        }
+        pending_.clear();
+        return cudaSuccess;
+    }
+    void totals(const std::string& name, double* ms, long long* count)
+    {
+        auto it = totals_.find(name);
+        *ms = it == totals_.end() ? 0.0 : it->second.ms;
+        *count = it == totals_.end() ? 0 : it->second.count;
+    }
+    void clear(bool destroy)
+    {
+        if (destroy) {
+            for (Pending& p : pending_) {
+                cudaEventDestroy(p.a);
+                cudaEventDestroy(p.b);
+            }
+            for (cudaEvent_t e : pool_) cudaEventDestroy(e);
+            pool_.clear();
+            pending_.clear();
+        }
+        totals_.clear();
+    }
+
+private:
+    struct Pending { std::string name; cudaEvent_t a, b; };
+    struct Total { double ms = 0; long long count = 0; };
+    cudaError_t take(cudaEvent_t* e)
+    {
+        if (!pool_.empty()) {
+            *e = pool_.back();
+            pool_.pop_back();
+            return cudaSuccess;
+        }
+        return cudaEventCreate(e);
+    }
+    std::vector<Pending> pending_;
+    std::vector<cudaEvent_t> pool_;
+    std::map<std::string, Total> totals_;
+};
+
+// Where one batch's kernels go: the RA kernel on `main`, the interneuron
+// kernel on `side` (forked from and joined back into main every interval, so
+// the two overlap); with a timer every launch runs on main, bracketed by events.
+struct LaunchCtx {
+    cudaStream_t main = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    KernelTimer* timer = nullptr;
+};
+
 template <class R>
-cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, cudaStream_t st);
+cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, const LaunchCtx& lc);
 
 template <class R>
 cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1, const RAStep<R>& rc,
-                            const IStep<R>& ic, cudaStream_t st);
+                            const IStep<R>& ic, const LaunchCtx& lc);
 
 }  // namespace ug

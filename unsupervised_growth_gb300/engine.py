@@ -24,7 +24,8 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
             "ug_free_network", "ug_run_test_trials", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
-            "ug_step_time", "ug_launch_count", "ug_calibrate_pipes"]
+            "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
+            "ug_calibrate_pipes"]
 
 
 class UGError(RuntimeError):
@@ -105,6 +106,8 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_neuron_state.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _f64p]
     L.ug_step_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p]
     L.ug_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.ug_set_kernel_timing.argtypes = [vp, C.c_int32]
+    L.ug_get_kernel_timing.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     for name in EXPORTED:
         if name not in ("ug_last_error", "ug_destroy"):
@@ -201,6 +204,15 @@ class Engine:
         n = C.c_int64(0)
         _check(self.L.ug_launch_count(self.ctx, C.byref(n)))
         return n.value
+
+    def set_kernel_timing(self, enabled: bool):
+        _check(self.L.ug_set_kernel_timing(self.ctx, 1 if enabled else 0))
+
+    def kernel_timing(self, kernel: str):
+        """(total device ms, launches) of one kernel since timing was enabled."""
+        ms, n = C.c_double(0), C.c_int64(0)
+        _check(self.L.ug_get_kernel_timing(self.ctx, kernel.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
 
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
