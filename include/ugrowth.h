@@ -118,6 +118,37 @@ ug_status ug_free_network(ug_ctx* ctx, int32_t net_id);
  * streams of trial index first_trial + k, all in one batched run. */
 ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials);
 
+/* Replaces the loop of chain_growth (NetworkGrowthSimulator.cpp:5763-5880): n_trials
+ * consecutive growth trials trial_1stSoma_pre_1stSoma_post_delays_fixedSpread (:8839-9571),
+ * trial k drawing the noise streams of trial index first_trial + k, each followed by
+ * check_bad_values, check_neuron_activity (:9573-9627), the maturation update
+ * (:2152-2183) and replace_neurons (:15869-15881).  Returns UG_ENUMERIC and stops when
+ * check_bad_values fails.  training: the training neurons get their kick (chainGrowth
+ * passes true). */
+ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials,
+                               int32_t training);
+/* Dense n_ra x n_ra RA->RA weights (weights_RA_RA). */
+ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out);
+/* Dense n_ra x n_ra axonal delays (axonal_delays_RA_RA). */
+ug_status ug_get_delays(ug_ctx* ctx, int32_t net_id, double* out);
+/* Ordered active (which 0) or super (which 1) synapse lists as CSR: offsets [n_ra + 1],
+ * targets [*total]; pass NULL arrays to query *total. */
+ug_status ug_get_synapse_list(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
+                              int64_t* total);
+/* Maturation state per RA neuron (rest_potential, GCa, mature, maturation_scale,
+ * remodeled, num_trials_after_replacement, firing_rate_long); any pointer may be NULL. */
+ug_status ug_get_neuron_props(ug_ctx* ctx, int32_t net_id, double* rest_potential, double* gca, int32_t* mature,
+                              double* maturation_scale, int32_t* remodeled, int32_t* trials_after_replacement,
+                              double* firing_rate_long);
+/* Neurons replaced after the last growth trial, in replacement order. */
+ug_status ug_get_replaced(ug_ctx* ctx, int32_t net_id, int32_t* out, int64_t capacity, int64_t* n_out);
+/* RA->I (which 0) or I->RA (which 1) connections as CSR over the source:
+ * offsets [n_src + 1], targets / weights / delays [*total]; NULL arrays query *total. */
+ug_status ug_get_connections(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
+                             double* weights, double* delays, int64_t* total);
+/* Neuron positions on the unit sphere, [n_ra][3] and [n_i][3]. */
+ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double* i_xyz);
+
 /* Per-instance spike statistics of the last batch: count and first step per neuron,
  * arrays [n_trials][n].  which: 0 somatic (HVC-RA), 1 dendritic (HVC-RA), 2 HVC-I. */
 ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* count, int32_t* first_step);

@@ -1,0 +1,498 @@
+// Growth trial: STDP, supersynapse and pruning rules of
+// NetworkGrowthSimulator::trial_1stSoma_pre_1stSoma_post_delays_fixedSpread
+// (c++/src/NetworkGrowthSimulator.cpp:8839-9571).
+//
+// The neuron integration and the RA->I / I->RA kicks are the interval kernels
+// of ug_trial.cuh.  Everything that touches the RA->RA synapses is kept in the
+// reference's order, because the ordered active / super lists and the Nss cap
+// depend on it:
+//  * k_growth_rows: one thread per presynaptic row i replays row i's delivery
+//    queue over the interval's steps.  A somatic spike of i opens a "stream"
+//    over its targets -- every j != i in the order of (delay, j) when i is
+//    unsaturated, its supersynapses when saturated (:8991-9030) -- and the
+//    streams are merged by (delivery time, target) exactly like the sorted
+//    std::vector queue (:9019-9027).  Each delivery kicks the target if the
+//    synapse is active and applies LTD against the target's recent
+//    post-synaptic events (:9069-9191).  Rows never touch each other's state,
+//    so rows run in parallel with the reference's semantics.
+//  * k_growth_newpost: builds the new post-synaptic event list of the interval
+//    in (step, neuron) order (:8952-8967) and appends the sync time (:9385).
+//  * k_growth_ltp: LTP/LTD of every row against the new post events and axon
+//    remodeling (:9392-9554).
+//  * k_growth_epilogue: potentiation_decay + update_all_synapses (:9567-9570).
+// Pre-synaptic events (per pair) and post-synaptic events (per neuron) are
+// gated 30 ms apart, so only the last 4 can fall inside the 100 ms STDP window:
+// small rings replace the reference's unbounded vectors.
+#pragma once
+#include "ug_trial.cuh"
+
+namespace ug {
+
+constexpr int kPreRing = 4;       // pre-synaptic events kept per pair
+constexpr int kPostRing = 8;      // post-synaptic events kept per neuron
+constexpr int kMaxStreams = 32;   // live delivery streams per row
+constexpr int kMaxNss = 16;       // largest supported Nss
+constexpr int kStreamOpen = 0;
+
+struct SynParams {
+    int Nss;
+    double A_P, A_D, T_0, T_P, T_D, TAU_P, TAU_D, BETA, BETA_SUPERSYNAPSE;
+    double ACTIVATION_THRESHOLD, SUPERSYNAPSE_THRESHOLD, WEIGHT_MAX;
+};
+
+// Device state of the RA->RA synapses of B growing networks of n neurons.
+struct GrowthDev {
+    int n, B;
+    SynParams sp;
+    double* W;              // [B][n][n] weights
+    const double* D;        // [B][n][n] axonal delays
+    const int* perm;        // [B][n][n-1] targets j != i sorted by (D_ij, j)
+    uint8_t* active;        // [B][n][n]
+    uint8_t* super;         // [B][n][n]
+    int* act_list;          // [B][n][n] ordered active targets
+    int* act_cnt;           // [B][n]
+    int* sup_list;          // [B][n][kMaxNss] ordered supersynapses
+    int* sup_cnt;           // [B][n]
+    int* remodeled;         // [B][n]
+    short* pre_step;        // [B][n][n][kPreRing] spike steps of the delivered pre events (time = T[step] + D)
+    uint8_t* pre_cnt;       // [B][n][n] events delivered so far (saturates at 255)
+    int* post_step;         // [B][n][kPostRing] sync steps of post events, ring
+    int* post_cnt;          // [B][n]
+    int* st_step;           // [B][n][kMaxStreams] spike step of each live stream
+    int* st_cursor;         // [B][n][kMaxStreams]
+    int* st_len;            // [B][n][kMaxStreams] targets in the stream (n-1, or the snapshot size)
+    int* st_tgt;            // [B][n][kMaxStreams][kMaxNss] snapshot of a saturated spike's targets
+    int* st_head;           // [B][n] first live stream (ring over kMaxStreams)
+    int* st_num;            // [B][n] live streams
+    int* newpost;           // [B][n * 16] new post events of the interval, in order
+    int* newpost_cnt;       // [B]
+    int* error;
+};
+
+__device__ __forceinline__ size_t gidx(const GrowthDev& g, int b, int i, int j)
+{
+    return ((size_t)b * g.n + i) * g.n + j;
+}
+
+// update_synapse, NetworkGrowthSimulator.cpp:16546-16592
+static __device__ __noinline__ void g_update_synapse(const GrowthDev& g, int b, int i, int j)
+{
+    const SynParams& sp = g.sp;
+    const size_t ij = gidx(g, b, i, j);
+    const size_t r = (size_t)b * g.n + i;
+    const double w = g.W[ij];
+    if ((w >= sp.ACTIVATION_THRESHOLD) && (g.active[ij] == 0) && (g.remodeled[r] == 0)) {
+        g.active[ij] = 1;
+        g.act_list[r * g.n + g.act_cnt[r]++] = j;
+    }
+    if ((w >= sp.SUPERSYNAPSE_THRESHOLD) && (g.super[ij] == 0) && (g.sup_cnt[r] < sp.Nss)) {
+        g.super[ij] = 1;
+        g.sup_list[r * kMaxNss + g.sup_cnt[r]++] = j;
+    }
+    if ((w < sp.SUPERSYNAPSE_THRESHOLD) && (g.super[ij] == 1)) {
+        g.super[ij] = 0;
+        g.remodeled[r] = 0;
+        int* L = g.sup_list + r * kMaxNss;
+        const int c = g.sup_cnt[r];
+        for (int k = 0; k < c; ++k)
+            if (L[k] == j) {
+                for (int m = k; m + 1 < c; ++m) L[m] = L[m + 1];
+                g.sup_cnt[r] = c - 1;
+                break;
+            }
+    }
+    if ((w < sp.ACTIVATION_THRESHOLD) && (g.active[ij] == 1)) {
+        g.active[ij] = 0;
+        int* L = g.act_list + r * g.n;
+        const int c = g.act_cnt[r];
+        for (int k = 0; k < c; ++k)
+            if (L[k] == j) {
+                for (int m = k; m + 1 < c; ++m) L[m] = L[m + 1];
+                g.act_cnt[r] = c - 1;
+                break;
+            }
+    }
+}
+
+// LTP / LTD, NetworkGrowthSimulator.cpp:16615-16652
+__device__ __forceinline__ void g_LTP(const SynParams& sp, double& w, double dt)
+{
+    if (dt <= sp.T_0) return;
+    if (dt <= sp.T_0 + sp.T_P)
+        w = w + sp.A_P * (dt - sp.T_0) / sp.T_P;
+    else
+        w = w + sp.A_P * exp(-(dt - sp.T_0 - sp.T_P) / sp.TAU_P);
+    if (w > sp.WEIGHT_MAX) w = sp.WEIGHT_MAX;
+    if (w < 0) w = 0;
+}
+
+__device__ __forceinline__ void g_LTD(const SynParams& sp, double& w, double dt)
+{
+    if (dt > sp.T_0) return;
+    if (dt >= sp.T_0 - sp.T_D)
+        w = w + w * sp.A_D * (dt - sp.T_0) / sp.T_D;
+    else
+        w = w - w * sp.A_D * exp((dt - sp.T_0 + sp.T_D) / sp.TAU_D);
+    if (w < 0) w = 0;
+}
+
+// axon_remodeling, NetworkGrowthSimulator.cpp:16363-16415
+static __device__ __noinline__ void g_axon_remodeling(const GrowthDev& g, int b, int i)
+{
+    const size_t r = (size_t)b * g.n + i;
+    for (int k = 0; k < g.act_cnt[r]; ++k) g.active[gidx(g, b, i, g.act_list[r * g.n + k])] = 0;
+    for (int k = 0; k < g.sup_cnt[r]; ++k) g.active[gidx(g, b, i, g.sup_list[r * kMaxNss + k])] = 1;
+    for (int k = 0; k < g.sup_cnt[r]; ++k) g.act_list[r * g.n + k] = g.sup_list[r * kMaxNss + k];
+    g.act_cnt[r] = g.sup_cnt[r];
+    g.remodeled[r] = 1;
+}
+
+// Number of the post events of neuron j kept in its ring (oldest first) and the k-th of them.
+__device__ __forceinline__ int post_num(const GrowthDev& g, int b, int j)
+{
+    const int c = g.post_cnt[(size_t)b * g.n + j];
+    return c < kPostRing ? c : kPostRing;
+}
+__device__ __forceinline__ int post_at(const GrowthDev& g, int b, int j, int k)
+{
+    const int c = g.post_cnt[(size_t)b * g.n + j];
+    const int first = c < kPostRing ? 0 : c - kPostRing;
+    return g.post_step[((size_t)b * g.n + j) * kPostRing + ((first + k) % kPostRing)];
+}
+
+// Delivery of one RA->RA event of row i to target j at step s (delivery time td).
+template <class R>
+static __device__ __noinline__ void g_deliver(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i, int j, int s,
+                          int spike_step, double td)
+{
+    const SynParams& sp = g.sp;
+    const size_t ij = gidx(g, b, i, j);
+    const size_t r = (size_t)b * g.n + i;
+    if (g.active[ij] == 1) {
+        // update_Ge_RA[target] += w, applied at the sync closing step s
+        const size_t slot = (size_t)(n.syncidx[s] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + j;
+        atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(g.W[ij] * kFixScale));
+    }
+    // new pre-synaptic event: first, or more than 30 ms after the previous one
+    const int pc = g.pre_cnt[ij];
+    bool new_pre = false;
+    if (pc == 0) {
+        new_pre = true;
+    } else {
+        const int last = g.pre_step[ij * kPreRing + ((pc - 1) % kPreRing)];
+        const double t_last = n.T[last] + g.D[ij];
+        if (td > t_last + 30.0) new_pre = true;
+    }
+    if (!new_pre) return;
+    g.pre_step[ij * kPreRing + (pc % kPreRing)] = (short)spike_step;
+    // at most one event per 30 ms: a 500 ms trial delivers <= 17 per pair
+    if (pc < 252) g.pre_cnt[ij] = (uint8_t)(pc + 1);
+    else atomicOr(g.error, kErrEventCapacity);
+    const double now = n.T[s];
+    const bool sat = g.sup_cnt[r] == sp.Nss;
+    if (sat && g.super[ij] != 1) {
+        // saturated: LTD only onto supersynapses; nothing changed, so no desaturation either
+        return;
+    }
+    const int np = post_num(g, b, j);
+    for (int k = 0; k < np; ++k) {
+        const double tp = n.T[post_at(g, b, j, k)];
+        if (!(tp >= now - 100.0)) continue;   // lower_bound(internal_time - STDP_WINDOW)
+        g_LTD(sp, g.W[ij], tp - td);
+        g_update_synapse(g, b, i, j);
+    }
+    if (sat && g.sup_cnt[r] < sp.Nss)
+        for (int jj = 0; jj < g.n; ++jj) g_update_synapse(g, b, i, jj);
+}
+
+// Row i's deliveries over steps s0..s1 (see the file comment).
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+{
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= g.n) return;
+    const size_t r = (size_t)b * g.n + i;
+    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    int head = g.st_head[r], num = g.st_num[r];
+    if (bits == 0 && num == 0) return;
+    int* stS = g.st_step + r * kMaxStreams;
+    int* stC = g.st_cursor + r * kMaxStreams;
+    int* stL = g.st_len + r * kMaxStreams;
+    int* stT = g.st_tgt + r * kMaxStreams * kMaxNss;
+    const int* perm = g.perm + r * (g.n - 1);
+    const double* Drow = g.D + r * g.n;
+    const int Nss = g.sp.Nss;
+    for (int s = s0; s <= s1; ++s) {
+        const double Ts = n.T[s];
+        if ((bits >> (s - s0)) & 1u) {
+            if (num >= kMaxStreams) {
+                atomicOr(g.error, kErrEventCapacity);
+            } else {
+                const int slot = (head + num) % kMaxStreams;
+                stS[slot] = s;
+                stC[slot] = 0;
+                const int sc = g.sup_cnt[r];
+                if (sc == Nss) {
+                    // saturated: deliver to the supersynapses only, sorted by (time, target)
+                    int* T = stT + slot * kMaxNss;
+                    for (int k = 0; k < sc; ++k) {
+                        const int t = g.sup_list[r * kMaxNss + k];
+                        const double tk = Ts + Drow[t];
+                        int m = k;
+                        while (m > 0) {
+                            const double tm = Ts + Drow[T[m - 1]];
+                            if (tm > tk || (tm == tk && T[m - 1] > t)) {
+                                T[m] = T[m - 1];
+                                --m;
+                            } else {
+                                break;
+                            }
+                        }
+                        T[m] = t;
+                    }
+                    stL[slot] = -sc;   // negative: snapshot stream
+                } else {
+                    stL[slot] = g.n - 1;
+                }
+                ++num;
+            }
+        }
+        // drain every stream head due at s, smallest (time, target) first
+        while (num > 0) {
+            int best = -1, bt_tgt = 0;
+            double bt_time = 0.0;
+            for (int q = 0; q < num; ++q) {
+                const int slot = (head + q) % kMaxStreams;
+                const int L = stL[slot];
+                const int c = stC[slot];
+                const int len = L < 0 ? -L : L;
+                if (c >= len) continue;
+                const int t = L < 0 ? stT[slot * kMaxNss + c] : perm[c];
+                const double td = n.T[stS[slot]] + Drow[t];
+                if (!(Ts >= td)) continue;
+                if (best < 0 || td < bt_time || (td == bt_time && t < bt_tgt)) {
+                    best = slot;
+                    bt_time = td;
+                    bt_tgt = t;
+                }
+            }
+            if (best < 0) break;
+            g_deliver(g, n, bt, b, i, bt_tgt, s, stS[best], bt_time);
+            ++stC[best];
+        }
+        // retire exhausted streams at the head of the ring
+        while (num > 0) {
+            const int L = stL[head];
+            if (stC[head] < (L < 0 ? -L : L)) break;
+            head = (head + 1) % kMaxStreams;
+            --num;
+        }
+    }
+    // exhausted streams behind a live one are retired when they reach the head
+    g.st_head[r] = head;
+    g.st_num[r] = num;
+}
+
+// New post-synaptic events of the interval in the reference's order: steps
+// ascending, neurons ascending within a step (:8952-8967), judged against the
+// post events recorded before this interval; then the sync time is appended
+// to each (:9385-9386).  One block per instance.
+template <class R>
+__global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+{
+    const int b = blockIdx.x;
+    __shared__ int cnt;
+    __shared__ int wsum[32];
+    if (threadIdx.x == 0) cnt = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int s = s0; s <= s1; ++s) {
+        const double Ts = n.T[s];
+        for (int base = 0; base < g.n; base += blockDim.x) {
+            const int i = base + threadIdx.x;
+            int flag = 0;
+            if (i < g.n) {
+                const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+                if ((bits >> (s - s0)) & 1u) {
+                    const int np = post_num(g, b, i);
+                    if (np == 0) flag = 1;
+                    else if (Ts > n.T[post_at(g, b, i, np - 1)] + 30.0) flag = 1;
+                }
+            }
+            // block-wide ordered compaction
+            const unsigned m = __ballot_sync(0xffffffffu, flag);
+            if (lane == 0) wsum[warp] = __popc(m);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int acc = cnt;
+                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+                    const int c = wsum[w];
+                    wsum[w] = acc;
+                    acc += c;
+                }
+                cnt = acc;
+            }
+            __syncthreads();
+            if (flag) {
+                const int pos = wsum[warp] + __popc(m & ((1u << lane) - 1u));
+                if (pos < g.n * 16) g.newpost[(size_t)b * g.n * 16 + pos] = i;
+                else atomicOr(g.error, kErrPostCapacity);
+            }
+            __syncthreads();
+        }
+    }
+    __syncthreads();
+    const int total = cnt < g.n * 16 ? cnt : g.n * 16;
+    if (threadIdx.x == 0) g.newpost_cnt[b] = total;
+    // append the sync time; a neuron listed twice gets two entries, in list order
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < total; ++k) {
+            const int j = g.newpost[(size_t)b * g.n * 16 + k];
+            const size_t rj = (size_t)b * g.n + j;
+            g.post_step[rj * kPostRing + (g.post_cnt[rj] % kPostRing)] = s1;
+            g.post_cnt[rj] += 1;
+        }
+    }
+}
+
+// LTP / LTD of every row against the interval's new post events, then axon
+// remodeling (NetworkGrowthSimulator.cpp:9392-9554).
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n, int s1)
+{
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= g.n) return;
+    const int total = g.newpost_cnt[b];
+    if (total == 0) return;
+    const SynParams& sp = g.sp;
+    const size_t r = (size_t)b * g.n + i;
+    const double now = n.T[s1];
+    const bool saturated = g.sup_cnt[r] == sp.Nss;
+    const int* list = g.newpost + (size_t)b * g.n * 16;
+    for (int k = 0; k < total; ++k) {
+        const int post = list[k];
+        if (post == i) continue;
+        if (saturated) {
+            bool found = false;
+            for (int m = 0; m < g.sup_cnt[r]; ++m) found |= g.sup_list[r * kMaxNss + m] == post;
+            if (!found) continue;
+        }
+        const size_t ij = gidx(g, b, i, post);
+        const int pc = g.pre_cnt[ij];
+        if (pc == 0) continue;
+        const int np = pc < kPreRing ? pc : kPreRing;
+        const double Dij = g.D[ij];
+        for (int q = 0; q < np; ++q) {
+            const int e = pc - np + q;
+            const double tpre = n.T[g.pre_step[ij * kPreRing + (e % kPreRing)]] + Dij;
+            if (!(tpre >= now - 100.0)) continue;
+            const double dt = now - tpre;
+            if (dt <= sp.T_0) g_LTD(sp, g.W[ij], dt);
+            else g_LTP(sp, g.W[ij], dt);
+            g_update_synapse(g, b, i, post);
+        }
+    }
+    if (g.sup_cnt[r] == sp.Nss && g.remodeled[r] == 0) g_axon_remodeling(g, b, i);
+}
+
+// potentiation_decay + update_all_synapses (:16346-16361, :16432-16443).
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
+{
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= g.n) return;
+    const SynParams& sp = g.sp;
+    double* Wr = g.W + ((size_t)b * g.n + i) * g.n;
+    for (int j = 0; j < g.n; ++j) {
+        double w = Wr[j];
+        if (w >= sp.SUPERSYNAPSE_THRESHOLD) w -= sp.BETA_SUPERSYNAPSE;
+        else w -= sp.BETA;
+        if (w < 0) w = 0;
+        Wr[j] = w;
+    }
+    for (int j = 0; j < g.n; ++j) g_update_synapse(g, b, i, j);
+}
+
+// Start of a growth trial: no streams, no pre or post events
+// (the reference's trial-local containers, :8869-8880).
+template <class R>
+__global__ void k_growth_reset(GrowthDev g)
+{
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nr = (size_t)g.B * g.n;
+    const size_t npair = nr * g.n;
+    for (size_t k = tid; k < npair; k += (size_t)gridDim.x * blockDim.x) g.pre_cnt[k] = 0;
+    for (size_t k = tid; k < nr; k += (size_t)gridDim.x * blockDim.x) {
+        g.post_cnt[k] = 0;
+        g.st_head[k] = 0;
+        g.st_num[k] = 0;
+    }
+}
+
+// remove_neurons_from_network, NetworkGrowthSimulator.cpp:15757-15859: every
+// row drops its synapses onto the replaced neurons (in list order), then the
+// replaced neurons' own rows are cleared.
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_growth_remove(GrowthDev g, const int* rep, int nrep)
+{
+    const int b = blockIdx.y;
+    const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (i >= g.n) return;
+    const size_t r = (size_t)b * g.n + i;
+    bool replaced = false;
+    for (int k = 0; k < nrep; ++k) {
+        const int j = rep[k];
+        replaced |= (j == i);
+        const size_t ij = gidx(g, b, i, j);
+        if (g.active[ij] == 1) {
+            int* L = g.act_list + r * g.n;
+            const int c = g.act_cnt[r];
+            for (int m = 0; m < c; ++m)
+                if (L[m] == j) {
+                    for (int q = m; q + 1 < c; ++q) L[q] = L[q + 1];
+                    g.act_cnt[r] = c - 1;
+                    break;
+                }
+            g.active[ij] = 0;
+        }
+        if (g.super[ij] == 1) {
+            int* L = g.sup_list + r * kMaxNss;
+            const int c = g.sup_cnt[r];
+            for (int m = 0; m < c; ++m)
+                if (L[m] == j) {
+                    for (int q = m; q + 1 < c; ++q) L[q] = L[q + 1];
+                    g.sup_cnt[r] = c - 1;
+                    break;
+                }
+            g.super[ij] = 0;
+            g.remodeled[r] = 0;
+        }
+        g.W[ij] = 0.0;
+    }
+    if (replaced) {
+        g.act_cnt[r] = 0;
+        g.sup_cnt[r] = 0;
+        g.remodeled[r] = 0;
+        for (int j = 0; j < g.n; ++j) {
+            const size_t ij = gidx(g, b, i, j);
+            g.super[ij] = 0;
+            g.active[ij] = 0;
+            g.W[ij] = 0.0;
+        }
+    }
+}
+
+// check_bad_values (HH2_test.cpp:244-260) over every RA neuron of every instance.
+template <class R>
+__global__ void k_check_bad(NetDev<R> n, BatchDev<R> bt, int* bad)
+{
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= (size_t)bt.B * n.n_ra) return;
+    const double vs = (double)bt.ra[0][k], vd = (double)bt.ra[1][k];
+    if (vs > 100 || vs < -200 || isnan(vs) || vd > 100 || vd < -200 || isnan(vd)) atomicOr(bad, 1);
+}
+
+}  // namespace ug

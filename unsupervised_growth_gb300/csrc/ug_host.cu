@@ -123,6 +123,13 @@ struct NetHost {
     std::vector<std::vector<int>> active, supers;
     std::vector<double> rest, gca, spread;
     std::vector<int> training;
+    // growth and replacement state (read_network_state, NetworkGrowthSimulator.cpp:1943-2020)
+    std::vector<double> L;                       // RA->RA synapse lengths
+    std::vector<double> ra2i_len, i2ra_len;
+    std::vector<int> mature, remodeled, tar;     // tar: trials after replacement
+    std::vector<double> scale, frl;              // maturation scale, firing_rate_long
+    std::vector<int> hist;                       // [n_ra][window] newest first
+    std::vector<double> ra_xyz, i_xyz;
 };
 
 class NetBase {
@@ -134,7 +141,14 @@ public:
     virtual ug_status spikes(int instance, int which, int32_t* neuron, int32_t* step, int64_t cap, int64_t* n,
                              cudaStream_t st) = 0;
     virtual ug_status neuron_state(int instance, int which, double* out, cudaStream_t st) = 0;
+    virtual ug_status run_growth_trials(uint32_t first_trial, int n_trials, int training, const ug::LaunchCtx& lc,
+                                        bool graphs, int64_t* launches) = 0;
+    virtual ug_status weights(double* out, cudaStream_t st) = 0;
+    virtual ug_status synapse_list(int which, int32_t* off, int32_t* tgt, int64_t* total, cudaStream_t st) = 0;
+    virtual ug_status neuron_props(double* rest, double* gca, int32_t* mature, double* scale, int32_t* remodeled,
+                                   int32_t* tar, double* frl, cudaStream_t st) = 0;
     NetHost h;
+    std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
     std::vector<int> sync_steps;    // step that closes each synchronization interval
     int ring = 0;
@@ -178,15 +192,29 @@ public:
     ug_status spikes(int instance, int which, int32_t* neuron, int32_t* step, int64_t cap, int64_t* n,
                      cudaStream_t st) override;
     ug_status neuron_state(int instance, int which, double* out, cudaStream_t st) override;
+    ug_status run_growth_trials(uint32_t first_trial, int n_trials, int training, const ug::LaunchCtx& lc, bool graphs,
+                                int64_t* launches) override;
+    ug_status weights(double* out, cudaStream_t st) override;
+    ug_status synapse_list(int which, int32_t* off, int32_t* tgt, int64_t* total, cudaStream_t st) override;
+    ug_status neuron_props(double* rest, double* gca, int32_t* mature, double* scale, int32_t* remodeled, int32_t* tar,
+                           double* frl, cudaStream_t st) override;
     ~NetImpl() override
     {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        if (ggraph_) cudaGraphExecDestroy(ggraph_);
     }
 
 private:
     ug_status ensure_batch(int B);
     ug_status check_error(cudaStream_t st);
     ug_status issue_batch(const ug::LaunchCtx& lc, int64_t* launches);
+    ug_status upload_connectivity(cudaStream_t st);
+    ug_status growth_init(cudaStream_t st);
+    ug_status issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launches);
+    ug_status after_growth_trial(uint32_t trial, cudaStream_t st);
+    ug_status replace_neurons(const std::vector<int>& rep, uint32_t trial, cudaStream_t st);
+    ug_status sync_static_lists(cudaStream_t st);
+    void drop_graphs();
 
     ug::NetDev<R> nd_{};
     ug::BatchDev<R> bd_{};
@@ -202,6 +230,15 @@ private:
     DevMem ring_ra_exc_, ring_ra_inh_, ring_i_exc_, spk_buf_, spk_count_, error_, trial_, mean_inj_;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_B_ = -1;
+    // growth
+    bool growth_ready_ = false;
+    bool rara_dirty_ = false;       // device synapse lists changed since the static lists were built
+    ug::GrowthDev gd_{};
+    DevMem gW_, gD_, gPerm_, gActive_, gSuper_, gActList_, gActCnt_, gSupList_, gSupCnt_, gRemod_, gPreStep_,
+        gPreCnt_, gPostStep_, gPostCnt_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
+        gNewpostCnt_, gSomaBits_, gBad_, gRep_;
+    cudaGraphExec_t ggraph_ = nullptr;
+    int ggraph_training_ = -1;
 };
 
 template <class R>
@@ -291,25 +328,39 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
         ic_.gi[k] = (R)std::exp(-hk / ug::IConst::tInh);
     }
 
-    // connectivity
-    CsrHost ri, ir, rr;
-    ri.off = H.ra2i_off; ri.tgt = H.ra2i_tgt; ri.d = H.ra2i_d;
-    for (double w : H.ra2i_w) ri.wq.push_back(to_fixed(w));
-    ir.off = H.i2ra_off; ir.tgt = H.i2ra_tgt; ir.d = H.i2ra_d;
-    for (double w : H.i2ra_w) ir.wq.push_back(to_fixed(w));
-    rr.off.assign(1, 0);
+    // growth and replacement state
+    const int win = H.mat.RATE_WINDOW_LONG;
+    H.L.assign(nn, 0.0);
+    if (d->len_rara) H.L.assign(d->len_rara, d->len_rara + nn);
+    H.ra2i_len.assign(e_ri, 0.0);
+    if (d->ra2i_len) H.ra2i_len.assign(d->ra2i_len, d->ra2i_len + e_ri);
+    H.i2ra_len.assign(e_ir, 0.0);
+    if (d->i2ra_len) H.i2ra_len.assign(d->i2ra_len, d->i2ra_len + e_ir);
+    H.mature.assign(NRA, 0);
+    if (d->mature) H.mature.assign(d->mature, d->mature + NRA);
+    H.remodeled.assign(NRA, 0);
+    if (d->remodeled) H.remodeled.assign(d->remodeled, d->remodeled + NRA);
+    H.tar.assign(NRA, 0);
+    if (d->trials_after_replacement) H.tar.assign(d->trials_after_replacement, d->trials_after_replacement + NRA);
+    H.scale.assign(NRA, 100000.0);
+    if (d->maturation_scale) H.scale.assign(d->maturation_scale, d->maturation_scale + NRA);
+    H.frl.assign(NRA, 0.0);
+    H.hist.assign((size_t)NRA * (win > 0 ? win : 0), 0);
+    if (d->activity_history && win > 0) H.hist.assign(d->activity_history, d->activity_history + (size_t)NRA * win);
+    H.ra_xyz.assign((size_t)3 * NRA, 0.0);
+    if (d->ra_xyz) H.ra_xyz.assign(d->ra_xyz, d->ra_xyz + (size_t)3 * NRA);
+    H.i_xyz.assign((size_t)3 * NI, 0.0);
+    if (d->i_xyz) H.i_xyz.assign(d->i_xyz, d->i_xyz + (size_t)3 * NI);
+
+    // delivery rings: deep enough for the largest delay, including the delays a
+    // replaced neuron can be given (arc length up to pi on the unit sphere)
     double max_delay = 0.0;
-    for (int i = 0; i < NRA; ++i) {
-        for (int j : H.active[i]) {
-            rr.tgt.push_back(j);
-            rr.wq.push_back(to_fixed(H.W[(size_t)i * NRA + j]));
-            rr.d.push_back(H.D[(size_t)i * NRA + j]);
-        }
-        rr.off.push_back((int)rr.tgt.size());
-    }
     for (double x : H.ra2i_d) max_delay = std::max(max_delay, x);
     for (double x : H.i2ra_d) max_delay = std::max(max_delay, x);
     for (double x : H.D) max_delay = std::max(max_delay, x);
+    if (H.conn.model_interneuron_distance > 0.0)
+        max_delay = std::max(max_delay, 3.14159265358979323846 * 40.0 / H.conn.model_interneuron_distance * 0.01 *
+                                            std::fabs(H.conn.delay_constant));
     if (!(max_delay >= 0.0) || max_delay > 1000.0) return fail(UG_EINVAL, "axonal delays must lie in [0, 1000] ms");
     ring = (int)std::floor(max_delay / 0.24) + 4;
 
@@ -324,9 +375,6 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
     std::vector<uint8_t> trn(NRA, 0);
     for (int id : H.training) trn[id] = 1;
     UG_TRY(dTraining_.upload(trn, st));
-    UG_TRY(ra2i_.upload(ri, st));
-    UG_TRY(i2ra_.upload(ir, st));
-    UG_TRY(rara_.upload(rr, st));
     UG_TRY(error_.alloc(sizeof(int)));
     UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
 
@@ -337,11 +385,52 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
     n.ra_decay = dRaDecay_.as<double>(); n.i_decay = dIDecay_.as<double>();
     n.Erest = dErest_.as<R>(); n.GCa = dGCa_.as<R>(); n.spread = dSpread_.as<double>();
     n.is_training = dTraining_.as<uint8_t>();
+    UG_TRY(upload_connectivity(st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+// Uploads the RA<->I connection lists and the static RA->RA lists (active
+// synapses with their weights, for test trials) from the host copy.
+template <class R>
+ug_status NetImpl<R>::upload_connectivity(cudaStream_t st)
+{
+    const NetHost& H = h;
+    const int NRA = H.n_ra;
+    CsrHost ri, ir, rr;
+    ri.off = H.ra2i_off; ri.tgt = H.ra2i_tgt; ri.d = H.ra2i_d;
+    for (double w : H.ra2i_w) ri.wq.push_back(to_fixed(w));
+    ir.off = H.i2ra_off; ir.tgt = H.i2ra_tgt; ir.d = H.i2ra_d;
+    for (double w : H.i2ra_w) ir.wq.push_back(to_fixed(w));
+    rr.off.assign(1, 0);
+    for (int i = 0; i < NRA; ++i) {
+        for (int j : H.active[i]) {
+            rr.tgt.push_back(j);
+            rr.wq.push_back(to_fixed(H.W[(size_t)i * NRA + j]));
+            rr.d.push_back(H.D[(size_t)i * NRA + j]);
+        }
+        rr.off.push_back((int)rr.tgt.size());
+    }
+    UG_TRY(ra2i_.upload(ri, st));
+    UG_TRY(i2ra_.upload(ir, st));
+    UG_TRY(rara_.upload(rr, st));
+    ug::NetDev<R>& n = nd_;
     n.ra2i_off = ra2i_.off.as<int>(); n.ra2i_tgt = ra2i_.tgt.as<int>(); n.ra2i_wq = ra2i_.wq.as<long long>(); n.ra2i_d = ra2i_.d.as<double>();
     n.i2ra_off = i2ra_.off.as<int>(); n.i2ra_tgt = i2ra_.tgt.as<int>(); n.i2ra_wq = i2ra_.wq.as<long long>(); n.i2ra_d = i2ra_.d.as<double>();
     n.rara_off = rara_.off.as<int>(); n.rara_tgt = rara_.tgt.as<int>(); n.rara_wq = rara_.wq.as<long long>(); n.rara_d = rara_.d.as<double>();
-    UG_CUDA(cudaStreamSynchronize(st));
+    drop_graphs();
     return UG_OK;
+}
+
+template <class R>
+void NetImpl<R>::drop_graphs()
+{
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    graph_exec_ = nullptr;
+    graph_B_ = -1;
+    if (ggraph_) cudaGraphExecDestroy(ggraph_);
+    ggraph_ = nullptr;
+    ggraph_training_ = -1;
 }
 
 template <class R>
@@ -368,11 +457,7 @@ ug_status NetImpl<R>::ensure_batch(int B)
     UG_TRY(trial_.alloc((size_t)B * sizeof(uint32_t)));
     UG_TRY(mean_inj_.alloc((size_t)B * sizeof(double)));
     B_cap_ = B;
-    if (graph_exec_) {
-        cudaGraphExecDestroy(graph_exec_);
-        graph_exec_ = nullptr;
-        graph_B_ = -1;
-    }
+    drop_graphs();
     ug::BatchDev<R>& b = bd_;
     for (int k = 0; k < 10; ++k) b.ra[k] = ra_[k].as<R>();
     b.ra_flags = ra_flags_.as<int>(); b.kick_step = kick_step_.as<int>(); b.ra_nsoma = ra_nsoma_.as<int>(); b.ra_ndend = ra_ndend_.as<int>();
@@ -412,7 +497,9 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
 {
     cudaStream_t st = lc.main;
     if (n_trials <= 0 || n_trials > 65535) return fail(UG_EINVAL, "n_trials must be in [1, 65535]");
+    if (rara_dirty_) UG_TRY(sync_static_lists(st));
     UG_TRY(ensure_batch(n_trials));
+    bd_.soma_bits = nullptr;
     bd_.B = n_trials;
     bd_.kick_on = 1;
     bd_.scatter_rara = 1;
@@ -513,6 +600,422 @@ ug_status NetImpl<R>::neuron_state(int instance, int which, double* out, cudaStr
         const R* src = (which == 0 ? ra_[f].as<R>() : iv_[f].as<R>()) + (size_t)instance * n;
         UG_CUDA(cudaMemcpy(tmp.data(), src, n * sizeof(R), cudaMemcpyDeviceToHost));
         for (int i = 0; i < n; ++i) out[(size_t)i * nf + f] = (double)tmp[i];
+    }
+    return UG_OK;
+}
+
+
+// ------------------------------------------------------------------ growth
+
+// Targets j != i of row i in the order (D_ij, j): the order in which a spike of
+// an unsaturated neuron reaches its targets (NetworkGrowthSimulator.cpp:9010-9030).
+static void sort_targets(const std::vector<double>& D, int n, std::vector<int>& perm)
+{
+    perm.assign((size_t)n * (n > 0 ? n - 1 : 0), 0);
+    std::vector<int> row(n > 0 ? n - 1 : 0);
+    for (int i = 0; i < n; ++i) {
+        int k = 0;
+        for (int j = 0; j < n; ++j)
+            if (j != i) row[k++] = j;
+        const double* Dr = D.data() + (size_t)i * n;
+        std::stable_sort(row.begin(), row.end(), [Dr](int a, int b) { return Dr[a] < Dr[b]; });
+        std::copy(row.begin(), row.end(), perm.begin() + (size_t)i * (n - 1));
+    }
+}
+
+template <class R>
+ug_status NetImpl<R>::growth_init(cudaStream_t st)
+{
+    const int n = h.n_ra;
+    if (h.syn.Nss < 0 || h.syn.Nss > ug::kMaxNss) return fail(UG_EINVAL, "Nss must lie in [0, 16]");
+    if (h.mat.RATE_WINDOW_LONG < 1000)
+        return fail(UG_EINVAL, "RATE_WINDOW_LONG must be >= 1000 (the 1000-trial robustness window reads it)");
+    const size_t nn = (size_t)n * n;
+    UG_TRY(gW_.upload(h.W, st));
+    UG_TRY(gD_.upload(h.D, st));
+    std::vector<int> perm;
+    sort_targets(h.D, n, perm);
+    UG_TRY(gPerm_.upload(perm, st));
+    std::vector<uint8_t> act(nn, 0), sup(nn, 0);
+    std::vector<int> al(nn, 0), ac(n, 0), sl((size_t)n * ug::kMaxNss, 0), sc(n, 0);
+    for (int i = 0; i < n; ++i) {
+        if ((int)h.supers[i].size() > h.syn.Nss) return fail(UG_EINVAL, "a super synapse list is longer than Nss");
+        for (int j : h.active[i]) {
+            act[(size_t)i * n + j] = 1;
+            al[(size_t)i * n + ac[i]++] = j;
+        }
+        for (int j : h.supers[i]) {
+            sup[(size_t)i * n + j] = 1;
+            sl[(size_t)i * ug::kMaxNss + sc[i]++] = j;
+        }
+    }
+    UG_TRY(gActive_.upload(act, st));
+    UG_TRY(gSuper_.upload(sup, st));
+    UG_TRY(gActList_.upload(al, st));
+    UG_TRY(gActCnt_.upload(ac, st));
+    UG_TRY(gSupList_.upload(sl, st));
+    UG_TRY(gSupCnt_.upload(sc, st));
+    UG_TRY(gRemod_.upload(h.remodeled, st));
+    UG_TRY(gPreStep_.alloc(nn * ug::kPreRing * sizeof(short)));
+    UG_TRY(gPreCnt_.alloc(nn));
+    UG_TRY(gPostStep_.alloc((size_t)n * ug::kPostRing * sizeof(int)));
+    UG_TRY(gPostCnt_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gStStep_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
+    UG_TRY(gStCur_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
+    UG_TRY(gStLen_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
+    UG_TRY(gStTgt_.alloc((size_t)n * ug::kMaxStreams * ug::kMaxNss * sizeof(int)));
+    UG_TRY(gStHead_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gStNum_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gNewpost_.alloc((size_t)n * 16 * sizeof(int)));
+    UG_TRY(gNewpostCnt_.alloc(sizeof(int)));
+    UG_TRY(gSomaBits_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gBad_.alloc(sizeof(int)));
+    UG_TRY(gRep_.alloc((size_t)n * sizeof(int)));
+    ug::GrowthDev& g = gd_;
+    g.n = n;
+    g.B = 1;
+    g.sp.Nss = h.syn.Nss;
+    g.sp.A_P = h.syn.A_P; g.sp.A_D = h.syn.A_D; g.sp.T_0 = h.syn.T_0; g.sp.T_P = h.syn.T_P; g.sp.T_D = h.syn.T_D;
+    g.sp.TAU_P = h.syn.TAU_P; g.sp.TAU_D = h.syn.TAU_D; g.sp.BETA = h.syn.BETA;
+    g.sp.BETA_SUPERSYNAPSE = h.syn.BETA_SUPERSYNAPSE; g.sp.ACTIVATION_THRESHOLD = h.syn.ACTIVATION_THRESHOLD;
+    g.sp.SUPERSYNAPSE_THRESHOLD = h.syn.SUPERSYNAPSE_THRESHOLD; g.sp.WEIGHT_MAX = h.syn.WEIGHT_MAX;
+    g.W = gW_.as<double>(); g.D = gD_.as<double>(); g.perm = gPerm_.as<int>();
+    g.active = gActive_.as<uint8_t>(); g.super = gSuper_.as<uint8_t>();
+    g.act_list = gActList_.as<int>(); g.act_cnt = gActCnt_.as<int>();
+    g.sup_list = gSupList_.as<int>(); g.sup_cnt = gSupCnt_.as<int>(); g.remodeled = gRemod_.as<int>();
+    g.pre_step = gPreStep_.as<short>(); g.pre_cnt = gPreCnt_.as<uint8_t>();
+    g.post_step = gPostStep_.as<int>(); g.post_cnt = gPostCnt_.as<int>();
+    g.st_step = gStStep_.as<int>(); g.st_cursor = gStCur_.as<int>(); g.st_len = gStLen_.as<int>();
+    g.st_tgt = gStTgt_.as<int>(); g.st_head = gStHead_.as<int>(); g.st_num = gStNum_.as<int>();
+    g.newpost = gNewpost_.as<int>(); g.newpost_cnt = gNewpostCnt_.as<int>();
+    g.error = error_.as<int>();
+    growth_ready_ = true;
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launches)
+{
+    int64_t cnt = 0;
+    UG_CUDA(ug::launch_trial_init<R>(nd_, bd_, lc));
+    cnt += 1 + (sizeof(R) == 4 ? 1 : 0);
+    UG_CUDA(ug::launch_growth_reset<R>(gd_, lc));
+    ++cnt;
+    const int Q = (int)sync_steps.size();
+    for (int q = 0; q < Q; ++q) {
+        const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
+        UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, lc));
+        UG_CUDA(ug::launch_growth_sync<R>(gd_, nd_, bd_, s0, sync_steps[q], lc));
+        cnt += 5;
+    }
+    UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
+    UG_CUDA(ug::launch_growth_epilogue<R>(gd_, lc));
+    cnt += 3;
+    if (launches) *launches += cnt;
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int training, const ug::LaunchCtx& lc,
+                                        bool graphs, int64_t* launches)
+{
+    cudaStream_t st = lc.main;
+    if (n_trials <= 0) return fail(UG_EINVAL, "n_trials must be positive");
+    if (!growth_ready_) UG_TRY(growth_init(st));
+    UG_TRY(ensure_batch(1));
+    bd_.B = 1;
+    bd_.kick_on = training ? 1 : 0;
+    bd_.scatter_rara = 0;
+    bd_.soma_bits = gSomaBits_.as<int>();
+    B_ = 1;
+    for (int t = 0; t < n_trials; ++t) {
+        const uint32_t trial = first_trial + (uint32_t)t;
+        // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
+        ug::HostStream hs{ug::make_stream(h.seed, ug::kNoiseTrial, (uint32_t)h.net_id, 0, trial), 0};
+        const double mean_inj = 100.0 + ug::random_G(300.0, hs.word());
+        UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), &trial, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+        UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), &mean_inj, sizeof(double), cudaMemcpyHostToDevice, st));
+        if (!graphs || lc.timer) {
+            UG_TRY(issue_growth_trial(lc, launches));
+        } else {
+            if (!ggraph_ || ggraph_training_ != bd_.kick_on) {
+                if (ggraph_) cudaGraphExecDestroy(ggraph_);
+                ggraph_ = nullptr;
+                cudaStream_t cap;
+                UG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+                cudaGraph_t g;
+                UG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+                ug::LaunchCtx clc = lc;
+                clc.main = cap;
+                int64_t dummy = 0;
+                ug_status s = issue_growth_trial(clc, &dummy);
+                cudaError_t e = cudaStreamEndCapture(cap, &g);
+                cudaStreamDestroy(cap);
+                if (s != UG_OK) return s;
+                UG_CUDA(e);
+                e = cudaGraphInstantiate(&ggraph_, g, 0);
+                cudaGraphDestroy(g);
+                UG_CUDA(e);
+                ggraph_training_ = bd_.kick_on;
+            }
+            UG_CUDA(cudaGraphLaunch(ggraph_, st));
+            int64_t n = 0;
+            ug::LaunchCtx none;
+            (void)none;
+            n = 3 + (sizeof(R) == 4 ? 1 : 0) + 5 * (int64_t)sync_steps.size() + 2;
+            if (launches) *launches += n;
+        }
+        // check_bad_values after the trial (:5794-5803)
+        UG_CUDA(cudaMemsetAsync(gBad_.as<int>(), 0, sizeof(int), st));
+        UG_CUDA(ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), st));
+        int bad = 0;
+        UG_CUDA(cudaMemcpyAsync(&bad, gBad_.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, st));
+        UG_TRY(check_error(st));
+        if (bad) return fail(UG_ENUMERIC, "bad values in the neuron dynamics (check_bad_values)");
+        rara_dirty_ = true;
+        UG_TRY(after_growth_trial(trial, st));
+    }
+    return UG_OK;
+}
+
+// The per-trial tail of chain_growth (NetworkGrowthSimulator.cpp:5841-5875):
+// trial counters, check_neuron_activity (:9573-9627), maturation
+// (update_neuron_properties_sameDendrite_diffMaturationRate, :2152-2183),
+// replacement (:15869-15881).  The next trial starts from set_to_rest.
+template <class R>
+ug_status NetImpl<R>::after_growth_trial(uint32_t trial, cudaStream_t st)
+{
+    const int n = h.n_ra;
+    const int W = h.mat.RATE_WINDOW_LONG;
+    std::vector<int> count(n);
+    UG_CUDA(cudaMemcpyAsync(count.data(), ra_nsoma_.as<int>(), n * sizeof(int), cudaMemcpyDeviceToHost, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i) h.tar[i] += 1;
+    std::vector<int> rep;
+    for (int i = 0; i < n; ++i) {
+        int* hi = h.hist.data() + (size_t)i * W;
+        std::memmove(hi + 1, hi, (size_t)(W - 1) * sizeof(int));   // push_front into the full circular buffer
+        hi[0] = count[i];
+        double sum = 0.0;
+        for (int k = 0; k < W; ++k) sum += hi[k];
+        h.frl[i] = sum / (double)W;
+        double robust = 0.0;
+        for (int k = 0; k < 1000; ++k)
+            if (hi[k] > 0) robust += 1;
+        robust = robust / 1000.0;
+        if (robust >= 0.5 && h.scale[i] != 1000.0) h.scale[i] = 1000.0;   // MATURATION_SCALE_DRIVEN
+        if (robust < h.mat.DEATH_RATE_THRESHOLD && h.tar[i] > 1000) rep.push_back(i);
+    }
+    for (int i = 0; i < n; ++i) {
+        if (h.mature[i] == 1) continue;
+        h.rest[i] = h.rest[i] + (h.rest[i] - h.mat.E_REST_MATURE) * (std::exp(-1.0 / h.scale[i]) - 1);
+        h.gca[i] = h.gca[i] + (h.gca[i] - h.mat.GCA_MATURE) * (std::exp(-1.0 / h.scale[i]) - 1);
+        if ((h.gca[i] >= h.mat.GCA_MATURE - 0.5) || (h.rest[i] <= h.mat.E_REST_MATURE - 0.5)) {
+            h.gca[i] = h.mat.GCA_MATURE;
+            h.rest[i] = h.mat.E_REST_MATURE;
+            h.mature[i] = 1;
+        }
+    }
+    replaced = rep;
+    if (!rep.empty()) UG_TRY(replace_neurons(rep, trial, st));
+    std::vector<R> er(h.rest.begin(), h.rest.end()), gc(h.gca.begin(), h.gca.end());
+    UG_CUDA(cudaMemcpyAsync(dErest_.as<R>(), er.data(), n * sizeof(R), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaMemcpyAsync(dGCa_.as<R>(), gc.data(), n * sizeof(R), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+static double sphere_dist(const double* a, const double* b)
+{
+    const double tmp = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    return tmp > 1.0 ? 0.0 : std::acos(tmp);
+}
+
+// replace_neurons: remove_neurons_from_network (:15757-15859) on the device,
+// then, on the host, sample_coordinates_for_replaced (:157-220),
+// sample_connectionsAndDelays_for_replaced (:528-618) and
+// update_replaced_neurons (:2109-2134), drawing from the trial's replacement
+// stream in the reference's order.
+template <class R>
+ug_status NetImpl<R>::replace_neurons(const std::vector<int>& rep, uint32_t trial, cudaStream_t st)
+{
+    const int n = h.n_ra, NI = h.n_i;
+    UG_CUDA(cudaMemcpyAsync(gRep_.as<int>(), rep.data(), rep.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    UG_CUDA(ug::launch_growth_remove<R>(gd_, gRep_.as<int>(), (int)rep.size(), st));
+
+    // connections as per-source lists
+    struct Conn { std::vector<int> tgt; std::vector<double> w, d, len; };
+    auto to_lists = [](const std::vector<int>& off, const std::vector<int>& tgt, const std::vector<double>& w,
+                       const std::vector<double>& d, const std::vector<double>& len, int nsrc) {
+        std::vector<Conn> c(nsrc);
+        for (int i = 0; i < nsrc; ++i)
+            for (int k = off[i]; k < off[i + 1]; ++k) {
+                c[i].tgt.push_back(tgt[k]); c[i].w.push_back(w[k]); c[i].d.push_back(d[k]); c[i].len.push_back(len[k]);
+            }
+        return c;
+    };
+    std::vector<Conn> ri = to_lists(h.ra2i_off, h.ra2i_tgt, h.ra2i_w, h.ra2i_d, h.ra2i_len, n);
+    std::vector<Conn> ir = to_lists(h.i2ra_off, h.i2ra_tgt, h.i2ra_w, h.i2ra_d, h.i2ra_len, NI);
+    for (int i = 0; i < NI; ++i)
+        for (int j : rep) {
+            Conn& c = ir[i];
+            auto it = std::find(c.tgt.begin(), c.tgt.end(), j);
+            if (it != c.tgt.end()) {
+                const size_t k = (size_t)(it - c.tgt.begin());
+                c.tgt.erase(it); c.w.erase(c.w.begin() + k); c.len.erase(c.len.begin() + k); c.d.erase(c.d.begin() + k);
+            }
+        }
+    for (int j : rep) ri[j] = Conn();
+
+    ug::HostStream rs{ug::make_stream(h.seed, ug::kNoiseReplace, (uint32_t)h.net_id, 0, trial), 0};
+    const double model = h.conn.model_interneuron_distance;
+    const double pi = 3.14159265358979323846;
+    const double too_close = model * 10.0 / 40.0;   // MIN_INTERSOMATIC_DISTANCE / EXPERIMENTAL_INTERNEURON_DISTANCE
+    std::vector<char> is_rep(n, 0);
+    for (int j : rep) is_rep[j] = 1;
+    std::vector<int> fixed;
+    for (int i = 0; i < n; ++i) if (!is_rep[i]) fixed.push_back(i);
+    double* X = h.ra_xyz.data();
+    const double* XI = h.i_xyz.data();
+    for (int r : rep) {
+        double p[3];
+        bool close = true;
+        while (close) {
+            close = false;
+            const double z = 2 * ug::random_G(1.0, rs.word()) - 1;
+            const double phi = ug::random_G(2.0 * pi, rs.word());
+            p[0] = std::sin(std::acos(z)) * std::cos(phi);
+            p[1] = std::sin(std::acos(z)) * std::sin(phi);
+            p[2] = z;
+            for (int j = 0; j < NI && !close; ++j) close = sphere_dist(p, XI + 3 * j) < too_close;
+            for (size_t f = 0; f < fixed.size() && !close; ++f) close = sphere_dist(p, X + 3 * fixed[f]) < too_close;
+        }
+        X[3 * r] = p[0]; X[3 * r + 1] = p[1]; X[3 * r + 2] = p[2];
+        fixed.push_back(r);
+    }
+    auto p_gauss = [](double A, double sigma, double d) { return A * std::exp(-d * d / (2 * (sigma * sigma))); };
+    const double dc = h.conn.delay_constant;
+    for (int id : rep)
+        for (int j = 0; j < NI; ++j) {
+            const double d = sphere_dist(X + 3 * id, XI + 3 * j) * 40.0 / model;
+            if (ug::random_G(1, rs.word()) < p_gauss(h.conn.A_RA2I, h.conn.SIGMA_RA2I, d)) {
+                const double G = ug::random_G(1.0, rs.word()) * h.conn.Gei_max;
+                ri[id].w.push_back(G); ri[id].tgt.push_back(j); ri[id].len.push_back(d);
+                ri[id].d.push_back(d * 0.01 * dc);
+            }
+        }
+    for (int i = 0; i < NI; ++i)
+        for (int id : rep) {
+            const double d = sphere_dist(XI + 3 * i, X + 3 * id) * 40.0 / model;
+            if (ug::random_G(1, rs.word()) < p_gauss(h.conn.B_I2RA, h.conn.SIGMA_I2RA, d)) {
+                const double G = ug::random_G(1.0, rs.word()) * h.conn.Gie_max;
+                ir[i].w.push_back(G); ir[i].tgt.push_back(id); ir[i].len.push_back(d);
+                ir[i].d.push_back(d * 0.01 * dc);
+            }
+        }
+    for (int i = 0; i < n; ++i)
+        for (int tg : rep) {
+            const double len = tg != i ? sphere_dist(X + 3 * i, X + 3 * tg) * 40.0 / model : 0.0;
+            h.L[(size_t)i * n + tg] = len;
+            h.D[(size_t)i * n + tg] = len * 0.01 * dc;
+        }
+    for (int src : rep)
+        for (int j = 0; j < n; ++j) {
+            const double len = j != src ? sphere_dist(X + 3 * src, X + 3 * j) * 40.0 / model : 0.0;
+            h.L[(size_t)src * n + j] = len;
+            h.D[(size_t)src * n + j] = len * 0.01 * dc;
+        }
+    auto to_csr = [](const std::vector<Conn>& c, std::vector<int>& off, std::vector<int>& tgt, std::vector<double>& w,
+                     std::vector<double>& d, std::vector<double>& len) {
+        off.assign(1, 0); tgt.clear(); w.clear(); d.clear(); len.clear();
+        for (const Conn& x : c) {
+            tgt.insert(tgt.end(), x.tgt.begin(), x.tgt.end()); w.insert(w.end(), x.w.begin(), x.w.end());
+            d.insert(d.end(), x.d.begin(), x.d.end()); len.insert(len.end(), x.len.begin(), x.len.end());
+            off.push_back((int)tgt.size());
+        }
+    };
+    to_csr(ri, h.ra2i_off, h.ra2i_tgt, h.ra2i_w, h.ra2i_d, h.ra2i_len);
+    to_csr(ir, h.i2ra_off, h.i2ra_tgt, h.i2ra_w, h.i2ra_d, h.i2ra_len);
+    for (int r : rep) {
+        h.rest[r] = h.mat.E_REST_IMMATURE;
+        h.gca[r] = h.mat.GCA_IMMATURE;
+        h.mature[r] = 0;
+        h.scale[r] = 100000.0;   // MATURATION_SCALE_SPONTANEOUS
+        h.tar[r] = 0;
+        std::fill(h.hist.begin() + (size_t)r * h.mat.RATE_WINDOW_LONG,
+                  h.hist.begin() + (size_t)(r + 1) * h.mat.RATE_WINDOW_LONG, 0);
+    }
+    // device copies of the delays, their target order and the RA<->I lists
+    UG_CUDA(cudaMemcpyAsync(gD_.as<double>(), h.D.data(), h.D.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    std::vector<int> perm;
+    sort_targets(h.D, n, perm);
+    UG_CUDA(cudaMemcpyAsync(gPerm_.as<int>(), perm.data(), perm.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    UG_TRY(upload_connectivity(st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+// Brings the host copy of the RA->RA state up to date with the device (after
+// growth trials) and rebuilds the static lists test trials deliver over.
+template <class R>
+ug_status NetImpl<R>::sync_static_lists(cudaStream_t st)
+{
+    const int n = h.n_ra;
+    std::vector<int> ac(n), al((size_t)n * n), sc(n), sl((size_t)n * ug::kMaxNss), rem(n);
+    UG_CUDA(cudaStreamSynchronize(st));
+    UG_CUDA(cudaMemcpy(h.W.data(), gW_.as<double>(), h.W.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    UG_CUDA(cudaMemcpy(ac.data(), gActCnt_.as<int>(), n * sizeof(int), cudaMemcpyDeviceToHost));
+    UG_CUDA(cudaMemcpy(al.data(), gActList_.as<int>(), al.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    UG_CUDA(cudaMemcpy(sc.data(), gSupCnt_.as<int>(), n * sizeof(int), cudaMemcpyDeviceToHost));
+    UG_CUDA(cudaMemcpy(sl.data(), gSupList_.as<int>(), sl.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    UG_CUDA(cudaMemcpy(rem.data(), gRemod_.as<int>(), n * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; ++i) {
+        h.active[i].assign(al.begin() + (size_t)i * n, al.begin() + (size_t)i * n + ac[i]);
+        h.supers[i].assign(sl.begin() + (size_t)i * ug::kMaxNss, sl.begin() + (size_t)i * ug::kMaxNss + sc[i]);
+    }
+    h.remodeled = rem;
+    rara_dirty_ = false;
+    return upload_connectivity(st);
+}
+
+template <class R>
+ug_status NetImpl<R>::weights(double* out, cudaStream_t st)
+{
+    if (rara_dirty_) UG_TRY(sync_static_lists(st));
+    std::memcpy(out, h.W.data(), h.W.size() * sizeof(double));
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::synapse_list(int which, int32_t* off, int32_t* tgt, int64_t* total, cudaStream_t st)
+{
+    if (rara_dirty_) UG_TRY(sync_static_lists(st));
+    const std::vector<std::vector<int>>& L = which == 0 ? h.active : h.supers;
+    int64_t t = 0;
+    for (int i = 0; i < h.n_ra; ++i) {
+        if (off) off[i] = (int32_t)t;
+        if (tgt) std::copy(L[i].begin(), L[i].end(), tgt + t);
+        t += (int64_t)L[i].size();
+    }
+    if (off) off[h.n_ra] = (int32_t)t;
+    if (total) *total = t;
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::neuron_props(double* rest, double* gca, int32_t* mature, double* scale, int32_t* remodeled,
+                                   int32_t* tar, double* frl, cudaStream_t st)
+{
+    if (rara_dirty_) UG_TRY(sync_static_lists(st));
+    for (int i = 0; i < h.n_ra; ++i) {
+        if (rest) rest[i] = h.rest[i];
+        if (gca) gca[i] = h.gca[i];
+        if (mature) mature[i] = h.mature[i];
+        if (scale) scale[i] = h.scale[i];
+        if (remodeled) remodeled[i] = h.remodeled[i];
+        if (tar) tar[i] = h.tar[i];
+        if (frl) frl[i] = h.frl[i];
     }
     return UG_OK;
 }
@@ -653,6 +1156,87 @@ ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, 
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaSetDevice(ctx->device));
     return n->run_test_trials(first_trial, n_trials, ctx->launch_ctx(), ctx->graphs, &ctx->launches);
+}
+
+ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials, int32_t training)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    UG_CUDA(cudaSetDevice(ctx->device));
+    return n->run_growth_trials(first_trial, n_trials, training, ctx->launch_ctx(), ctx->graphs, &ctx->launches);
+}
+
+ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (!out) return fail(UG_EINVAL, "null output");
+    return n->weights(out, ctx->stream);
+}
+
+ug_status ug_get_delays(ug_ctx* ctx, int32_t net_id, double* out)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (!out) return fail(UG_EINVAL, "null output");
+    std::memcpy(out, n->h.D.data(), n->h.D.size() * sizeof(double));
+    return UG_OK;
+}
+
+ug_status ug_get_synapse_list(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
+                              int64_t* total)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (which != 0 && which != 1) return fail(UG_EINVAL, "which must be 0 or 1");
+    return n->synapse_list(which, offsets, targets, total, ctx->stream);
+}
+
+ug_status ug_get_neuron_props(ug_ctx* ctx, int32_t net_id, double* rest_potential, double* gca, int32_t* mature,
+                              double* maturation_scale, int32_t* remodeled, int32_t* trials_after_replacement,
+                              double* firing_rate_long)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    return n->neuron_props(rest_potential, gca, mature, maturation_scale, remodeled, trials_after_replacement,
+                           firing_rate_long, ctx->stream);
+}
+
+ug_status ug_get_replaced(ug_ctx* ctx, int32_t net_id, int32_t* out, int64_t capacity, int64_t* n_out)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (n_out) *n_out = (int64_t)n->replaced.size();
+    for (int64_t k = 0; out && k < capacity && k < (int64_t)n->replaced.size(); ++k) out[k] = n->replaced[(size_t)k];
+    return UG_OK;
+}
+
+ug_status ug_get_connections(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
+                             double* weights, double* delays, int64_t* total)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (which != 0 && which != 1) return fail(UG_EINVAL, "which must be 0 or 1");
+    const NetHost& H = n->h;
+    const std::vector<int>& off = which == 0 ? H.ra2i_off : H.i2ra_off;
+    const std::vector<int>& tgt = which == 0 ? H.ra2i_tgt : H.i2ra_tgt;
+    const std::vector<double>& w = which == 0 ? H.ra2i_w : H.i2ra_w;
+    const std::vector<double>& d = which == 0 ? H.ra2i_d : H.i2ra_d;
+    if (total) *total = (int64_t)tgt.size();
+    if (offsets) std::copy(off.begin(), off.end(), offsets);
+    if (targets) std::copy(tgt.begin(), tgt.end(), targets);
+    if (weights) std::copy(w.begin(), w.end(), weights);
+    if (delays) std::copy(d.begin(), d.end(), delays);
+    return UG_OK;
+}
+
+ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double* i_xyz)
+{
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (ra_xyz) std::copy(n->h.ra_xyz.begin(), n->h.ra_xyz.end(), ra_xyz);
+    if (i_xyz) std::copy(n->h.i_xyz.begin(), n->h.i_xyz.end(), i_xyz);
+    return UG_OK;
 }
 
 ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* count, int32_t* first_step)

@@ -5,4 +5,10 @@ namespace ug {
 template cudaError_t launch_trial_init<float>(const NetDev<float>&, const BatchDev<float>&, const LaunchCtx&);
 template cudaError_t launch_interval<float>(const NetDev<float>&, const BatchDev<float>&, int, int, int,
                                             const RAStep<float>&, const IStep<float>&, const LaunchCtx&);
+template cudaError_t launch_growth_reset<float>(const GrowthDev&, const LaunchCtx&);
+template cudaError_t launch_growth_sync<float>(const GrowthDev&, const NetDev<float>&, const BatchDev<float>&, int, int,
+                                             const LaunchCtx&);
+template cudaError_t launch_growth_epilogue<float>(const GrowthDev&, const LaunchCtx&);
+template cudaError_t launch_growth_remove<float>(const GrowthDev&, const int*, int, cudaStream_t);
+template cudaError_t launch_check_bad<float>(const NetDev<float>&, const BatchDev<float>&, int*, cudaStream_t);
 }  // namespace ug

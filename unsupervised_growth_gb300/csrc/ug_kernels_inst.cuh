@@ -96,4 +96,48 @@ cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int
     return cudaGetLastError();
 }
 
+template <class R>
+cudaError_t launch_growth_reset(const GrowthDev& g, const LaunchCtx& lc)
+{
+    UG_TIMED(lc, "k_growth_reset", (k_growth_reset<R><<<1024, 256, 0, lc.main>>>(g)));
+    return cudaGetLastError();
+}
+
+// Deliveries of the interval's RA spikes to RA targets, then the sync's post
+// events, LTP and axon remodeling.
+template <class R>
+cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int s0, int s1,
+                               const LaunchCtx& lc)
+{
+    const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
+    UG_TIMED(lc, "k_growth_rows", (k_growth_rows<R><<<rows, kBlock, 0, lc.main>>>(g, n, b, s0, s1)));
+    UG_TIMED(lc, "k_growth_newpost", (k_growth_newpost<R><<<g.B, 1024, 0, lc.main>>>(g, n, b, s0, s1)));
+    UG_TIMED(lc, "k_growth_ltp", (k_growth_ltp<R><<<rows, kBlock, 0, lc.main>>>(g, n, s1)));
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc)
+{
+    const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
+    UG_TIMED(lc, "k_growth_epilogue", (k_growth_epilogue<R><<<rows, kBlock, 0, lc.main>>>(g)));
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st)
+{
+    const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
+    k_growth_remove<R><<<rows, kBlock, 0, st>>>(g, rep, nrep);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad, cudaStream_t st)
+{
+    const size_t total = (size_t)b.B * n.n_ra;
+    k_check_bad<R><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(n, b, bad);
+    return cudaGetLastError();
+}
+
 }  // namespace ug

@@ -8,7 +8,7 @@
 #include <string>
 #include <vector>
 
-#include "ug_trial.cuh"
+#include "ug_growth.cuh"
 
 namespace ug {
 
@@ -99,5 +99,18 @@ cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, const La
 template <class R>
 cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1, const RAStep<R>& rc,
                             const IStep<R>& ic, const LaunchCtx& lc);
+
+// Growth trial pieces (ug_growth.cuh).
+template <class R>
+cudaError_t launch_growth_reset(const GrowthDev& g, const LaunchCtx& lc);
+template <class R>
+cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int s0, int s1,
+                               const LaunchCtx& lc);
+template <class R>
+cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc);
+template <class R>
+cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st);
+template <class R>
+cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad, cudaStream_t st);
 
 }  // namespace ug

@@ -23,7 +23,9 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
-            "ug_free_network", "ug_run_test_trials", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
+            "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_get_weights", "ug_get_delays",
+            "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
+            "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
             "ug_calibrate_pipes"]
 
@@ -102,6 +104,14 @@ def load_library(path: str = LIB_PATH):
     L.ug_free_network.argtypes = [vp, C.c_int32]
     L.ug_run_test_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32]
     L.ug_get_trial_stats.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p]
+    L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
+    L.ug_get_weights.argtypes = [vp, C.c_int32, _f64p]
+    L.ug_get_delays.argtypes = [vp, C.c_int32, _f64p]
+    L.ug_get_synapse_list.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p, C.POINTER(C.c_int64)]
+    L.ug_get_neuron_props.argtypes = [vp, C.c_int32, _f64p, _f64p, _i32p, _f64p, _i32p, _i32p, _f64p]
+    L.ug_get_replaced.argtypes = [vp, C.c_int32, _i32p, C.c_int64, C.POINTER(C.c_int64)]
+    L.ug_get_connections.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p, _f64p, _f64p, C.POINTER(C.c_int64)]
+    L.ug_get_coordinates.argtypes = [vp, C.c_int32, _f64p, _f64p]
     L.ug_get_spikes.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.POINTER(C.c_int64)]
     L.ug_get_neuron_state.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, _f64p]
     L.ug_step_time.argtypes = [vp, C.c_int32, C.c_int32, _f64p]
@@ -137,6 +147,64 @@ class ResidentNetwork:
         """n_trials independent test trials (trial_no_stdp_fixedSpread), noise streams first_trial + k."""
         _check(self.engine.L.ug_run_test_trials(self.engine.ctx, self.id, first_trial, n_trials))
         self.batch = n_trials
+
+    def run_growth_trials(self, first_trial: int, n_trials: int, training: bool = True):
+        """n_trials consecutive growth trials, each followed by the between-trial bookkeeping."""
+        _check(self.engine.L.ug_run_growth_trials(self.engine.ctx, self.id, first_trial, n_trials, 1 if training else 0))
+        self.batch = 1
+
+    def weights(self):
+        w = np.zeros((self.n_ra, self.n_ra))
+        _check(self.engine.L.ug_get_weights(self.engine.ctx, self.id, _p(w, _f64p)))
+        return w
+
+    def delays(self):
+        d = np.zeros((self.n_ra, self.n_ra))
+        _check(self.engine.L.ug_get_delays(self.engine.ctx, self.id, _p(d, _f64p)))
+        return d
+
+    def synapse_list(self, which: int):
+        """which 0 active, 1 super -> list of per-row ordered target lists."""
+        tot = C.c_int64(0)
+        _check(self.engine.L.ug_get_synapse_list(self.engine.ctx, self.id, which, None, None, C.byref(tot)))
+        off = np.zeros(self.n_ra + 1, dtype=np.int32)
+        tgt = np.zeros(max(tot.value, 1), dtype=np.int32)
+        _check(self.engine.L.ug_get_synapse_list(self.engine.ctx, self.id, which, _p(off, _i32p), _p(tgt, _i32p),
+                                                 C.byref(tot)))
+        return [tgt[off[i]:off[i + 1]].tolist() for i in range(self.n_ra)]
+
+    def neuron_props(self):
+        N = self.n_ra
+        rest, gca, scale, frl = (np.zeros(N) for _ in range(4))
+        mature, remod, tar = (np.zeros(N, dtype=np.int32) for _ in range(3))
+        _check(self.engine.L.ug_get_neuron_props(self.engine.ctx, self.id, _p(rest, _f64p), _p(gca, _f64p),
+                                                 _p(mature, _i32p), _p(scale, _f64p), _p(remod, _i32p),
+                                                 _p(tar, _i32p), _p(frl, _f64p)))
+        return dict(rest_potential=rest, gca=gca, mature=mature, maturation_scale=scale, remodeled=remod,
+                    trials_after_replacement=tar, firing_rate_long=frl)
+
+    def replaced(self):
+        n = C.c_int64(0)
+        _check(self.engine.L.ug_get_replaced(self.engine.ctx, self.id, None, 0, C.byref(n)))
+        out = np.zeros(n.value, dtype=np.int32)
+        _check(self.engine.L.ug_get_replaced(self.engine.ctx, self.id, _p(out, _i32p), n.value, C.byref(n)))
+        return out
+
+    def connections(self, which: int):
+        n_src = self.n_ra if which == 0 else self.n_i
+        tot = C.c_int64(0)
+        _check(self.engine.L.ug_get_connections(self.engine.ctx, self.id, which, None, None, None, None, C.byref(tot)))
+        off = np.zeros(n_src + 1, dtype=np.int32)
+        t = tot.value
+        tgt, w, d = np.zeros(max(t, 1), dtype=np.int32), np.zeros(max(t, 1)), np.zeros(max(t, 1))
+        _check(self.engine.L.ug_get_connections(self.engine.ctx, self.id, which, _p(off, _i32p), _p(tgt, _i32p),
+                                                _p(w, _f64p), _p(d, _f64p), C.byref(tot)))
+        return off, tgt[:t], w[:t], d[:t]
+
+    def coordinates(self):
+        ra, ii = np.zeros((self.n_ra, 3)), np.zeros((self.n_i, 3))
+        _check(self.engine.L.ug_get_coordinates(self.engine.ctx, self.id, _p(ra, _f64p), _p(ii, _f64p)))
+        return ra, ii
 
     def trial_stats(self, which: int):
         """(count, first_step) arrays [n_trials][n]; which 0 soma, 1 dendrite, 2 interneuron."""
