@@ -170,6 +170,22 @@ ug_status ug_launch_count(ug_ctx* ctx, int64_t* n);
 ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled);
 ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches);
 
+/* No counterpart in the reference.  One single-precision test trial of a loaded network
+ * (as ug_run_test_trials with n_trials = 1) that allocates no device memory, for callers
+ * that cannot call cudaMalloc: a serving loop working inside a fixed HBM budget or that
+ * must not stall other streams (cudaMalloc/cudaFree can synchronize the device), or a host
+ * whose device memory belongs to another allocator.  Its scratch lives in a 4 MiB static
+ * device array that every GPU loading this library holds until exit; networks needing more
+ * (a network of 1000 HVC(RA) and 250 HVC(I) neurons with delays up to 10 ms fits) get UG_EINVAL.  Outputs are caller-owned device
+ * arrays: soma/dend count and first step [n_ra], interneuron count and first step [n_i].
+ * The first call on a device resolves the array's address (make it before any stream
+ * capture).  Every call shares the array: calls that overlap on the GPU race.  Returns
+ * after the trial has finished; UG_EINVAL for a double-precision context or when growth
+ * trials ran since the last ug_run_test_trials on this network. */
+ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint32_t trial, int32_t* soma_count,
+                                    int32_t* soma_first, int32_t* dend_count, int32_t* dend_first,
+                                    int32_t* inter_count, int32_t* inter_first);
+
 /* No counterpart in the reference (measurement support): measured throughput of the
  * SFU (ex2/rcp approximations, operations per second) and of FP32 FMA on `device`,
  * the denominators of the integrators' roofline. */

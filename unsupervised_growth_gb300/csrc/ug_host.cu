@@ -16,6 +16,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <memory>
 #include <string>
 #include <vector>
@@ -147,6 +148,10 @@ public:
     virtual ug_status synapse_list(int which, int32_t* off, int32_t* tgt, int64_t* total, cudaStream_t st) = 0;
     virtual ug_status neuron_props(double* rest, double* gca, int32_t* mature, double* scale, int32_t* remodeled,
                                    int32_t* tar, double* frl, cudaStream_t st) = 0;
+    // Device view of a single-precision network for ug_run_test_trial_noalloc; false
+    // for double-precision networks or when growth trials changed the RA->RA lists
+    // since they were last uploaded.
+    virtual bool f32_view(ug::NetDev<float>* out) const { (void)out; return false; }
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -202,6 +207,16 @@ public:
     {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (ggraph_) cudaGraphExecDestroy(ggraph_);
+    }
+    bool f32_view(ug::NetDev<float>* out) const override
+    {
+        if constexpr (sizeof(R) == 4) {
+            *out = nd_;
+            return !rara_dirty_;
+        } else {
+            (void)out;
+            return false;
+        }
     }
 
 private:
@@ -1301,3 +1316,164 @@ ug_status ug_launch_count(ug_ctx* ctx, int64_t* out)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------
+// Test trial without device allocation.
+//
+// Some callers cannot call cudaMalloc: a serving loop that runs inside a fixed,
+// pre-planned HBM budget, or that must not stall other streams (cudaMalloc and
+// cudaFree can synchronize the whole device), and hosts whose device memory is
+// owned by another allocator.  ug_run_test_trial_noalloc takes all of its
+// scratch -- neuron state, delivery rings, noise events, spike records -- from
+// the file-scope array below, which every GPU that loads this library holds
+// until the process exits.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = (size_t)4 << 20;   // 4 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[64] = {};   // device address of the array, per device ordinal
+
+// Sets `ptr` to the array's device address on the current device, resolving it
+// once per device (the host-side name of the array is not a device address).
+ug_status noalloc_scratch(int device, unsigned char** ptr)
+{
+    if (device < 0 || device >= 64) return fail(UG_EINVAL, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[device]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(UG_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_addr[device] = p;
+    }
+    *ptr = static_cast<unsigned char*>(g_noalloc_addr[device]);
+    return UG_OK;
+}
+
+// Bump allocator over the scratch array (256-byte aligned pieces).
+struct Carve {
+    unsigned char* base;
+    size_t used = 0;
+    template <class T>
+    T* take(size_t count)
+    {
+        const size_t off = (used + 255) & ~(size_t)255;
+        used = off + count * sizeof(T);
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
+__global__ void k_noalloc_begin(uint32_t* trial_slot, double* mean_inj_slot, int* error_slot, uint32_t trial)
+{
+    *trial_slot = trial;
+    *mean_inj_slot = 100.0;   // test trials inject at 100 ms (NetworkGrowthSimulator.cpp:12785)
+    *error_slot = 0;
+}
+
+}  // namespace
+
+extern "C" ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint32_t trial, int32_t* soma_count,
+                                               int32_t* soma_first, int32_t* dend_count, int32_t* dend_first,
+                                               int32_t* inter_count, int32_t* inter_first)
+{
+    NetBase* net;
+    UG_TRY(get_net(ctx, net_id, &net));
+    if (!soma_count || !soma_first || !dend_count || !dend_first || !inter_count || !inter_first)
+        return fail(UG_EINVAL, "every output must be a device array");
+    ug::NetDev<float> nd;
+    if (!net->f32_view(&nd))
+        return fail(UG_EINVAL, "the no-allocation test trial needs a single-precision network whose RA->RA lists "
+                               "are current (run ug_run_test_trials once after growth trials)");
+    UG_CUDA(cudaSetDevice(ctx->device));
+    unsigned char* base = nullptr;
+    UG_TRY(noalloc_scratch(ctx->device, &base));
+
+    const int nra = nd.n_ra, ni = nd.n_i;
+    const int ev_cap = (int)(nd.num_steps * 0.02 * 0.25 * 2.0) + 64;   // noise events per channel, as the batched path
+    const int spk_cap = 16 * (2 * nra + ni);
+    Carve c{base};
+    ug::BatchDev<float> b{};
+    b.B = 1;
+    b.kick_on = 1;
+    b.scatter_rara = 1;
+    b.soma_bits = nullptr;
+    uint32_t* trial_slot = c.take<uint32_t>(1);
+    double* mean_slot = c.take<double>(1);
+    b.trial = trial_slot;
+    b.mean_inj = mean_slot;
+    b.error = c.take<int>(1);
+    for (int k = 0; k < 10; ++k) b.ra[k] = c.take<float>(nra);
+    b.ra_flags = c.take<int>(nra);
+    b.kick_step = c.take<int>(nra);
+    b.ra_nsoma = c.take<int>(nra);
+    b.ra_ndend = c.take<int>(nra);
+    b.ra_first_soma = c.take<int>(nra);
+    b.ra_first_dend = c.take<int>(nra);
+    for (int k = 0; k < 7; ++k) b.iv[k] = c.take<float>(ni);
+    b.i_noise = c.take<double>(2 * (size_t)ni);
+    b.i_noise_step = c.take<int>(2 * (size_t)ni);
+    b.i_events = c.take<int2>(2 * (size_t)ni * ev_cap);
+    b.i_ev_idx = c.take<int>(2 * (size_t)ni);
+    b.ev_cap = ev_cap;
+    b.i_word = c.take<uint32_t>(ni);
+    b.i_flag = c.take<int>(ni);
+    b.i_nspk = c.take<int>(ni);
+    b.i_first = c.take<int>(ni);
+    b.ring_ra_exc = c.take<long long>((size_t)nd.ring * nra);
+    b.ring_ra_inh = c.take<long long>((size_t)nd.ring * nra);
+    b.ring_i_exc = c.take<long long>((size_t)nd.ring * ni);
+    b.spk_buf = c.take<int2>(spk_cap);
+    b.spk_count = c.take<int>(1);
+    b.spk_cap = spk_cap;
+    if (c.used > kNoAllocScratchBytes)
+        return fail(UG_EINVAL, "network too large for the no-allocation test trial: it needs " + std::to_string(c.used) +
+                                   " bytes of scratch, the static array holds " +
+                                   std::to_string(kNoAllocScratchBytes));
+
+    ug::LaunchCtx lc;
+    lc.main = ctx->stream;
+    k_noalloc_begin<<<1, 1, 0, lc.main>>>(trial_slot, mean_slot, b.error, trial);
+    UG_CUDA(cudaGetLastError());
+    // every piece that must start at zero is set by k_trial_init (state, rings, counters)
+    UG_CUDA(ug::launch_trial_init<float>(nd, b, lc));
+    const std::vector<int>& ss = net->sync_steps;
+    const int Q = (int)ss.size();
+    ug::RAStep<float> rc{};
+    ug::IStep<float> ic{};
+    const NetHost& H = net->h;
+    rc.dt = 0.02f;
+    rc.sq = (float)std::sqrt(0.02);
+    rc.sig_s = (float)H.noise.white_noise_std_soma;
+    rc.sig_d = (float)H.noise.white_noise_std_dend;
+    rc.mu_s = (float)H.noise.white_noise_mean_soma;
+    rc.mu_d = (float)H.noise.white_noise_mean_dend;
+    rc.e1 = (float)std::exp(-0.02 / ug::RAConst::tau);
+    rc.e2 = (float)std::exp(-0.01 / ug::RAConst::tau);
+    ic.dt = 0.02f;
+    const double cnum[12] = {UG_DP_CNUM}, cden[12] = {UG_DP_CDEN};
+    for (int k = 0; k < 12; ++k) {
+        const double hk = k == 0 ? 0.0 : k == 11 ? 0.02 : cnum[k] * 0.02 / cden[k];
+        ic.ge[k] = (float)std::exp(-hk / ug::IConst::tExc);
+        ic.gi[k] = (float)std::exp(-hk / ug::IConst::tInh);
+    }
+    for (int q = 0; q < Q; ++q) {
+        const int s0 = q == 0 ? 1 : ss[q - 1] + 1;
+        UG_CUDA(ug::launch_interval<float>(nd, b, q, s0, ss[q], rc, ic, lc));
+    }
+    UG_CUDA(ug::launch_interval<float>(nd, b, Q, nd.num_steps, nd.num_steps - 1, rc, ic, lc));
+    ctx->launches += 2 * ((int64_t)Q + 1) + 3;
+    const size_t ra_bytes = (size_t)nra * sizeof(int), i_bytes = (size_t)ni * sizeof(int);
+    UG_CUDA(cudaMemcpyAsync(soma_count, b.ra_nsoma, ra_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    UG_CUDA(cudaMemcpyAsync(soma_first, b.ra_first_soma, ra_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    UG_CUDA(cudaMemcpyAsync(dend_count, b.ra_ndend, ra_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    UG_CUDA(cudaMemcpyAsync(dend_first, b.ra_first_dend, ra_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    UG_CUDA(cudaMemcpyAsync(inter_count, b.i_nspk, i_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    UG_CUDA(cudaMemcpyAsync(inter_first, b.i_first, i_bytes, cudaMemcpyDeviceToDevice, lc.main));
+    int err = 0;
+    UG_CUDA(cudaMemcpyAsync(&err, b.error, sizeof(int), cudaMemcpyDeviceToHost, lc.main));
+    UG_CUDA(cudaStreamSynchronize(lc.main));
+    if (err) return fail(UG_ECAPACITY, "a spike or noise-event buffer of the no-allocation trial overflowed");
+    return UG_OK;
+}

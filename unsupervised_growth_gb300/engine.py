@@ -27,7 +27,7 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
-            "ug_calibrate_pipes"]
+            "ug_run_test_trial_noalloc", "ug_calibrate_pipes"]
 
 
 class UGError(RuntimeError):
@@ -118,6 +118,7 @@ def load_library(path: str = LIB_PATH):
     L.ug_launch_count.argtypes = [vp, C.POINTER(C.c_int64)]
     L.ug_set_kernel_timing.argtypes = [vp, C.c_int32]
     L.ug_get_kernel_timing.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.ug_run_test_trial_noalloc.argtypes = [vp, C.c_int32, C.c_uint32] + [C.c_void_p] * 6
     L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     for name in EXPORTED:
         if name not in ("ug_last_error", "ug_destroy"):
