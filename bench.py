@@ -40,6 +40,10 @@ SEED = 3
 #   I : 12 stages x 63 ops + 376 ops of the DP8 tableau sums      = 1132 FP32 ops; 12 x (4 ex2 + 1 rcp) = 60 SFU
 FP32_RA, FP32_I = 488, 1132
 MUFU_RA, MUFU_I = 40, 60
+# DRAM bytes per launch of the dominant kernel from the committed ncu capture
+# (profiles/k_interval_integrators_128trials_full.md: 16.4 MB read, ~0 written at
+# 128 trials), scaled to a launch of BATCH trials: the state read grows with the trials.
+DRAM_BYTES_RA_PER_TRIAL = 16.4e6 / 128
 CPU_SAMPLE_STEPS = 6000   # first 120 ms of a trial (includes the training kick at 100 ms)
 
 
@@ -262,7 +266,9 @@ def run_ours(args, rank, world, local_rank):
             "e2e": {"value": e2e_value, "unit": "trials/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fma_peak / 1e12, "unit": "T FP32 ops/s",
-                         "frac": achieved / fma_peak, "traffic": None, "kernel": dom,
+                         "frac": achieved / fma_peak, "kernel": dom,
+                         "traffic": DRAM_BYTES_RA_PER_TRIAL * BATCH if dom == "k_interval_ra" else None,
+                         "traffic_source": "ncu capture of 128 trials scaled by the trials per launch",
                          "peak_source": "FP32 FMA throughput loop (ug_calibrate_pipes), measured in this run; "
                                         "SFU peak (ex2+rcp loop) also measured",
                          "sfu_peak_gops": mufu_peak / 1e9, "kernels": kernels,
