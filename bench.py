@@ -294,6 +294,69 @@ def run_ours(args, rank, world, local_rank):
     return result
 
 
+def make_growth_network():
+    from unsupervised_growth_gb300.network import synthetic_growth_network
+    return synthetic_growth_network(n_ra=N_RA, n_i=N_I, n_tr=10, seed=2, delays="lognormal", lognormal_mean=3.0,
+                                    lognormal_sigma=1.5, delay_cap=10.0)
+
+
+def run_growth(args, local_rank):
+    """Growth at scale: one network, consecutive growth trials (a step is one trial
+    together with its between-trial bookkeeping).  Single-precision neurons with
+    double-precision weights, against the plain double-precision path."""
+    import torch
+
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    B.build()
+    torch.cuda.set_device(local_rank)
+    net = make_growth_network()
+    eng = Engine(precision=32, device=local_rank)
+    rn = eng.load_network(net)
+    rn.run_growth_trials(0, args.warmup, True)
+    eng.synchronize()
+    eng.set_kernel_timing(False)
+    l0 = eng.launch_count()
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        rn.run_growth_trials(args.warmup, args.steps, True)
+        eng.synchronize()
+        wall = time.perf_counter() - t0
+    launches = eng.launch_count() - l0
+    sup32 = [sorted(x) for x in rn.synapse_list(1)]
+    eng.set_kernel_timing(True)
+    rn.run_growth_trials(args.warmup + args.steps, 1, True)
+    names = ("k_interval_ra", "k_interval_i", "k_growth_rows", "k_growth_newpost", "k_growth_ltp",
+             "k_growth_epilogue", "k_trial_init", "k_noise_events", "k_growth_reset")
+    kt = {k: eng.kernel_timing(k) for k in names}
+    eng.set_kernel_timing(False)
+    result = {"metric": "growth trials/s (500 ms growth trials, 2000 RA + 550 I network, one network)",
+              "value": args.steps / wall, "unit": "trials/s", "n_gpus": 1, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+              "dtype": "f32 neurons, f64 weights", "data": "synthetic (seeded network and Philox noise)",
+              "config": {"workload": "growth trials of one 2000 HVC-RA + 550 HVC-I sphere network, lognormal "
+                                     "delays mean 3 ms capped 10 ms, 10 training neurons"},
+              "neuron_steps_per_s": args.steps / wall * (N_RA + N_I) * (NUM_STEPS - 1),
+              "gpu_launches": launches, "clocks": clk.summary(),
+              "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()}}
+    if not args.skip_fp64:
+        eng64 = Engine(precision=64, device=local_rank, use_graphs=False)
+        rn64 = eng64.load_network(net)
+        t0 = time.perf_counter()
+        rn64.run_growth_trials(0, args.warmup + args.steps, True)
+        eng64.synchronize()
+        fp64_wall = time.perf_counter() - t0
+        sup64 = [sorted(x) for x in rn64.synapse_list(1)]
+        result["fp64_plain_gpu"] = {"trials_per_s": (args.warmup + args.steps) / fp64_wall,
+                                    "how": "double precision, no graph, same trials"}
+        result["same_supersynapse_topology_as_fp64"] = sup32 == sup64
+        rn64.free()
+        eng64.close()
+    rn.free()
+    eng.close()
+    return result
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -322,6 +385,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="test", choices=["test", "growth"],
+                    help="test: batched test trials (the headline); growth: consecutive growth trials of one network")
     ap.add_argument("--batch", type=int, default=BATCH, help="test trials per step (profiling runs use fewer)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
@@ -332,6 +397,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         res = run_reference(args, rank)
+    elif args.workload == "growth":
+        res = run_growth(args, local_rank) if rank == 0 else None
     else:
         res = run_ours(args, rank, world, local_rank)
     if rank == 0 and res is not None:

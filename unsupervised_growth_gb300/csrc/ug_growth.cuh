@@ -6,7 +6,7 @@
 // of ug_trial.cuh.  Everything that touches the RA->RA synapses is kept in the
 // reference's order, because the ordered active / super lists and the Nss cap
 // depend on it:
-//  * k_growth_rows: one thread per presynaptic row i replays row i's delivery
+//  * k_growth_rows: one warp per presynaptic row i replays row i's delivery
 //    queue over the interval's steps.  A somatic spike of i opens a "stream"
 //    over its targets -- every j != i in the order of (delay, j) when i is
 //    unsaturated, its supersynapses when saturated (:8991-9030) -- and the
@@ -205,12 +205,99 @@ static __device__ __noinline__ void g_deliver(const GrowthDev& g, const NetDev<R
         for (int jj = 0; jj < g.n; ++jj) g_update_synapse(g, b, i, jj);
 }
 
-// Row i's deliveries over steps s0..s1 (see the file comment).
-template <class R>
-__global__ void __launch_bounds__(kBlock) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+// Opens the delivery stream of a somatic spike of row r at step s: every
+// target j != i in (delay, j) order when the row is unsaturated, otherwise its
+// supersynapses sorted by (delivery time, target) (:8991-9030).
+__device__ __forceinline__ int g_open_stream(const GrowthDev& g, size_t r, int s, double Ts, const double* Drow,
+                                             int head, int num, int* stS, int* stC, int* stL, int* stT)
 {
+    if (num >= kMaxStreams) {
+        atomicOr(g.error, kErrEventCapacity);
+        return num;
+    }
+    const int slot = (head + num) % kMaxStreams;
+    stS[slot] = s;
+    stC[slot] = 0;
+    const int sc = g.sup_cnt[r];
+    if (sc == g.sp.Nss) {
+        int* T = stT + slot * kMaxNss;
+        for (int k = 0; k < sc; ++k) {
+            const int t = g.sup_list[r * kMaxNss + k];
+            const double tk = Ts + Drow[t];
+            int m = k;
+            while (m > 0) {
+                const double tm = Ts + Drow[T[m - 1]];
+                if (tm > tk || (tm == tk && T[m - 1] > t)) {
+                    T[m] = T[m - 1];
+                    --m;
+                } else {
+                    break;
+                }
+            }
+            T[m] = t;
+        }
+        stL[slot] = -sc;   // negative length: snapshot stream
+    } else {
+        stL[slot] = g.n - 1;
+    }
+    return num + 1;
+}
+
+// Drains row i's events due at step s one by one, smallest (time, target)
+// first: the reference's order, used when a step holds more due events than
+// the warp's merge buffer.
+template <class R>
+__device__ void g_drain_seq(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i, int s,
+                            double Ts, int head, int num, const int* stS, int* stC, const int* stL, const int* stT,
+                            const int* perm, const double* Drow)
+{
+    while (num > 0) {
+        int best = -1, bt_tgt = 0;
+        double bt_time = 0.0;
+        for (int q = 0; q < num; ++q) {
+            const int slot = (head + q) % kMaxStreams;
+            const int L = stL[slot];
+            const int c = stC[slot];
+            const int len = L < 0 ? -L : L;
+            if (c >= len) continue;
+            const int t = L < 0 ? stT[slot * kMaxNss + c] : perm[c];
+            const double td = n.T[stS[slot]] + Drow[t];
+            if (!(Ts >= td)) continue;
+            if (best < 0 || td < bt_time || (td == bt_time && t < bt_tgt)) {
+                best = slot;
+                bt_time = td;
+                bt_tgt = t;
+            }
+        }
+        if (best < 0) break;
+        g_deliver(g, n, bt, b, i, bt_tgt, s, stS[best], bt_time);
+        ++stC[best];
+    }
+}
+
+constexpr int kRowWarps = 4;    // rows (warps) per block
+constexpr int kDueCap = 256;    // due events merged per step in shared memory
+
+// Row i's deliveries over steps s0..s1, one warp per row.  Each step the warp
+// gathers every due event of the row's streams (each stream's due events are a
+// prefix of its remaining targets), ranks them by (delivery time, target) --
+// the order of the reference's sorted queue -- and processes them 32 at a time.
+// An event whose processing cannot change the row's state (no activation,
+// deactivation or supersynapse change, no desaturation) touches only its own
+// pair, so such events commit in parallel; at the first event that would
+// change state (or a repeated target) the warp falls back to the exact
+// one-event path for that event and continues after it.
+template <class R>
+__global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0,
+                                                                int s1)
+{
+    __shared__ double sh_td[kRowWarps][2][kDueCap];
+    __shared__ int sh_t[kRowWarps][2][kDueCap];
+    __shared__ int sh_sp[kRowWarps][2][kDueCap];
+    __shared__ int sh_newc[kRowWarps][kMaxStreams];
     const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * kRowWarps + w;
     if (i >= g.n) return;
     const size_t r = (size_t)b * g.n + i;
     const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
@@ -222,64 +309,148 @@ __global__ void __launch_bounds__(kBlock) k_growth_rows(GrowthDev g, NetDev<R> n
     int* stT = g.st_tgt + r * kMaxStreams * kMaxNss;
     const int* perm = g.perm + r * (g.n - 1);
     const double* Drow = g.D + r * g.n;
-    const int Nss = g.sp.Nss;
+    const SynParams& sp = g.sp;
+    double* btd = sh_td[w][0];
+    int* bt_t = sh_t[w][0];
+    int* bsp = sh_sp[w][0];
+    double* otd = sh_td[w][1];
+    int* ot = sh_t[w][1];
+    int* osp = sh_sp[w][1];
     for (int s = s0; s <= s1; ++s) {
         const double Ts = n.T[s];
         if ((bits >> (s - s0)) & 1u) {
-            if (num >= kMaxStreams) {
-                atomicOr(g.error, kErrEventCapacity);
-            } else {
-                const int slot = (head + num) % kMaxStreams;
-                stS[slot] = s;
-                stC[slot] = 0;
-                const int sc = g.sup_cnt[r];
-                if (sc == Nss) {
-                    // saturated: deliver to the supersynapses only, sorted by (time, target)
-                    int* T = stT + slot * kMaxNss;
-                    for (int k = 0; k < sc; ++k) {
-                        const int t = g.sup_list[r * kMaxNss + k];
-                        const double tk = Ts + Drow[t];
-                        int m = k;
-                        while (m > 0) {
-                            const double tm = Ts + Drow[T[m - 1]];
-                            if (tm > tk || (tm == tk && T[m - 1] > t)) {
-                                T[m] = T[m - 1];
-                                --m;
-                            } else {
-                                break;
-                            }
-                        }
-                        T[m] = t;
-                    }
-                    stL[slot] = -sc;   // negative: snapshot stream
-                } else {
-                    stL[slot] = g.n - 1;
-                }
-                ++num;
-            }
+            if (lane == 0) num = g_open_stream(g, r, s, Ts, Drow, head, num, stS, stC, stL, stT);
+            num = __shfl_sync(0xffffffffu, num, 0);
+            __syncwarp();
         }
-        // drain every stream head due at s, smallest (time, target) first
-        while (num > 0) {
-            int best = -1, bt_tgt = 0;
-            double bt_time = 0.0;
-            for (int q = 0; q < num; ++q) {
-                const int slot = (head + q) % kMaxStreams;
-                const int L = stL[slot];
-                const int c = stC[slot];
-                const int len = L < 0 ? -L : L;
-                if (c >= len) continue;
-                const int t = L < 0 ? stT[slot * kMaxNss + c] : perm[c];
-                const double td = n.T[stS[slot]] + Drow[t];
-                if (!(Ts >= td)) continue;
-                if (best < 0 || td < bt_time || (td == bt_time && t < bt_tgt)) {
-                    best = slot;
-                    bt_time = td;
-                    bt_tgt = t;
+        // gather the due events of every stream
+        int total = 0;
+        bool overflow = false;
+        for (int q = 0; q < num && !overflow; ++q) {
+            const int slot = (head + q) % kMaxStreams;
+            const int L = stL[slot];
+            const int len = L < 0 ? -L : L;
+            int c = stC[slot];
+            const int spk = stS[slot];
+            const double Tsp = n.T[spk];
+            while (c < len) {
+                const int idx = c + lane;
+                bool due = false;
+                double td = 0.0;
+                int t = 0;
+                if (idx < len) {
+                    t = L < 0 ? stT[slot * kMaxNss + idx] : perm[idx];
+                    td = Tsp + Drow[t];
+                    due = Ts >= td;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, due);
+                const int nd = __popc(m);   // delivery times rise along a stream: the due set is a prefix
+                if (total + nd > kDueCap) {
+                    overflow = true;
+                    break;
+                }
+                if (due) {
+                    btd[total + lane] = td;
+                    bt_t[total + lane] = t;
+                    bsp[total + lane] = spk;
+                }
+                total += nd;
+                c += nd;
+                if (nd < 32) break;
+            }
+            if (lane == 0) sh_newc[w][q] = c;
+        }
+        __syncwarp();
+        if (overflow) {
+            // more due events than the buffer holds: the exact one-by-one drain
+            if (lane == 0) g_drain_seq(g, n, bt, b, i, s, Ts, head, num, stS, stC, stL, stT, perm, Drow);
+            __syncwarp();
+        } else if (total > 0) {
+            for (int q = lane; q < num; q += 32) stC[(head + q) % kMaxStreams] = sh_newc[w][q];
+            // rank by (time, target, position): distinct keys, so ranks are a permutation
+            for (int e = lane; e < total; e += 32) {
+                const double te = btd[e];
+                const int ge = bt_t[e];
+                int rank = 0;
+                for (int f = 0; f < total; ++f) {
+                    const double tf = btd[f];
+                    const int gf = bt_t[f];
+                    rank += (tf < te) || (tf == te && (gf < ge || (gf == ge && f < e)));
+                }
+                otd[rank] = te;
+                ot[rank] = ge;
+                osp[rank] = bsp[e];
+            }
+            __syncwarp();
+            int base = 0;
+            while (base < total) {
+                const int e = base + lane;
+                const bool has = e < total;
+                const int rem = g.remodeled[r];
+                const int sc = g.sup_cnt[r];
+                const bool sat = sc == sp.Nss;
+                bool changing = false, do_write = false, new_pre = false, is_active = false;
+                double wv = 0.0, w2 = 0.0, td = 0.0;
+                int t = -1, spk = 0, pc = 0;
+                size_t ij = 0;
+                if (has) {
+                    td = otd[e];
+                    t = ot[e];
+                    spk = osp[e];
+                    ij = gidx(g, b, i, t);
+                    is_active = g.active[ij] == 1;
+                    const bool su = g.super[ij] == 1;
+                    wv = g.W[ij];
+                    pc = g.pre_cnt[ij];
+                    if (pc == 0) {
+                        new_pre = true;
+                    } else {
+                        const int last = g.pre_step[ij * kPreRing + ((pc - 1) % kPreRing)];
+                        new_pre = td > n.T[last] + g.D[ij] + 30.0;
+                    }
+                    w2 = wv;
+                    if (new_pre && (!sat || su)) {
+                        const double now = Ts;
+                        const int np = post_num(g, b, t);
+                        for (int k = 0; k < np; ++k) {
+                            const double tp = n.T[post_at(g, b, t, k)];
+                            if (!(tp >= now - 100.0)) continue;
+                            g_LTD(sp, w2, tp - td);
+                            do_write = true;
+                            changing |= (w2 >= sp.ACTIVATION_THRESHOLD && !is_active && rem == 0) ||
+                                        (w2 >= sp.SUPERSYNAPSE_THRESHOLD && !su && sc < sp.Nss) ||
+                                        (w2 < sp.SUPERSYNAPSE_THRESHOLD && su) ||
+                                        (w2 < sp.ACTIVATION_THRESHOLD && is_active);
+                        }
+                    }
+                    // a target twice in one chunk goes through the exact path
+                    const unsigned same = __match_any_sync(__activemask(), t);
+                    if (__popc(same) > 1 && lane != __ffs(same) - 1) changing = true;
+                }
+                const unsigned chg = __ballot_sync(0xffffffffu, has && changing);
+                const int nchunk = min(32, total - base);
+                const int f = chg ? __ffs(chg) - 1 : nchunk;
+                if (has && lane < f) {
+                    if (is_active) {
+                        const size_t slot = (size_t)(n.syncidx[s] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + t;
+                        atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(wv * kFixScale));
+                    }
+                    if (new_pre) {
+                        g.pre_step[ij * kPreRing + (pc % kPreRing)] = (short)spk;
+                        if (pc < 252) g.pre_cnt[ij] = (uint8_t)(pc + 1);
+                        else atomicOr(g.error, kErrEventCapacity);
+                    }
+                    if (do_write) g.W[ij] = w2;
+                }
+                __syncwarp();
+                if (f < nchunk) {
+                    if (lane == 0) g_deliver(g, n, bt, b, i, ot[base + f], s, osp[base + f], otd[base + f]);
+                    __syncwarp();
+                    base += f + 1;
+                } else {
+                    base += nchunk;
                 }
             }
-            if (best < 0) break;
-            g_deliver(g, n, bt, b, i, bt_tgt, s, stS[best], bt_time);
-            ++stC[best];
         }
         // retire exhausted streams at the head of the ring
         while (num > 0) {
@@ -288,10 +459,12 @@ __global__ void __launch_bounds__(kBlock) k_growth_rows(GrowthDev g, NetDev<R> n
             head = (head + 1) % kMaxStreams;
             --num;
         }
+        __syncwarp();
     }
-    // exhausted streams behind a live one are retired when they reach the head
-    g.st_head[r] = head;
-    g.st_num[r] = num;
+    if (lane == 0) {
+        g.st_head[r] = head;
+        g.st_num[r] = num;
+    }
 }
 
 // New post-synaptic events of the interval in the reference's order: steps
@@ -304,6 +477,13 @@ __global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> 
     const int b = blockIdx.x;
     __shared__ int cnt;
     __shared__ int wsum[32];
+    // most intervals hold no somatic spike at all
+    int any = 0;
+    for (int i = threadIdx.x; i < g.n; i += blockDim.x) any |= bt.soma_bits[(size_t)b * n.n_ra + i];
+    if (!__syncthreads_or(any)) {
+        if (threadIdx.x == 0) g.newpost_cnt[b] = 0;
+        return;
+    }
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
