@@ -275,30 +275,237 @@ __device__ void g_drain_seq(const GrowthDev& g, const NetDev<R>& n, const BatchD
     }
 }
 
-constexpr int kRowWarps = 4;    // rows (warps) per block
-constexpr int kDueCap = 256;    // due events merged per step in shared memory
+constexpr int kRowWarps = 2;    // rows (warps) per block (2 x RowShared stays under 48 KB)
+constexpr int kDueCap = 512;    // due events merged per segment in shared memory
+constexpr int kSegSteps = 32;   // longest interval the row kernel handles
 
-// Row i's deliveries over steps s0..s1, one warp per row.  Each step the warp
-// gathers every due event of the row's streams (each stream's due events are a
-// prefix of its remaining targets), ranks them by (delivery time, target) --
-// the order of the reference's sorted queue -- and processes them 32 at a time.
-// An event whose processing cannot change the row's state (no activation,
-// deactivation or supersynapse change, no desaturation) touches only its own
-// pair, so such events commit in parallel; at the first event that would
-// change state (or a repeated target) the warp falls back to the exact
-// one-event path for that event and continues after it.
+// Per-warp shared buffers of the row kernel.
+struct RowShared {
+    double td[2][kDueCap];     // gathered / ranked delivery times
+    int tgt[2][kDueCap];
+    int spk[2][kDueCap];       // spike step of the event's stream (streams are in spike order)
+    int newc[kMaxStreams];     // stream cursors after the gather
+    int rs[kMaxStreams + 1];   // start of each stream's run in the gather buffer
+};
+
+// Gathers every event of row r due by Tlim: each stream's due events are a
+// prefix of its remaining targets (delivery times rise along a stream).
+// Returns the event count, or -1 when they do not fit; cursors are committed
+// only on success.  nrun = streams that contributed events.
+template <class R>
+__device__ __forceinline__ int g_gather(const GrowthDev& g, const NetDev<R>& n, double Tlim, int head, int num,
+                                        const int* stS, int* stC, const int* stL, const int* stT, const int* perm,
+                                        const double* Drow, RowShared& sh, int lane, int& nrun)
+{
+    int total = 0;
+    nrun = 0;
+    for (int q = 0; q < num; ++q) {
+        const int slot = (head + q) % kMaxStreams;
+        const int L = stL[slot];
+        const int len = L < 0 ? -L : L;
+        int c = stC[slot];
+        const int spk = stS[slot];
+        const double Tsp = n.T[spk];
+        const int start = total;
+        while (c < len) {
+            const int idx = c + lane;
+            bool due = false;
+            double td = 0.0;
+            int t = 0;
+            if (idx < len) {
+                t = L < 0 ? stT[slot * kMaxNss + idx] : perm[idx];
+                td = Tsp + Drow[t];
+                due = Tlim >= td;
+            }
+            const int nd = __popc(__ballot_sync(0xffffffffu, due));
+            if (total + nd > kDueCap) return -1;
+            if (due) {
+                sh.td[0][total + lane] = td;
+                sh.tgt[0][total + lane] = t;
+                sh.spk[0][total + lane] = spk;
+            }
+            total += nd;
+            c += nd;
+            if (nd < 32) break;
+        }
+        if (lane == 0) sh.newc[q] = c;
+        if (total > start) {
+            if (lane == 0) sh.rs[nrun] = start;
+            ++nrun;
+        }
+    }
+    if (lane == 0) sh.rs[nrun] = total;
+    __syncwarp();
+    for (int q = lane; q < num; q += 32) stC[(head + q) % kMaxStreams] = sh.newc[q];
+    return total;
+}
+
+// Event order of the reference's queue: (delivery time, target), earlier spike first on a tie.
+__device__ __forceinline__ bool ev_less(double ta, int ga, int sa, double tb, int gb, int sb)
+{
+    return ta < tb || (ta == tb && (ga < gb || (ga == gb && sa < sb)));
+}
+
+// Ranks the gathered events into buffer 1 in queue order.  Runs are merged by
+// binary search; a run whose (time, target) order differs from its (delay,
+// target) order (delivery times that round equal) takes the quadratic rank.
+__device__ __forceinline__ void g_rank(RowShared& sh, int total, int nrun, int lane)
+{
+    bool sorted = true;
+    for (int e = lane; e + 1 < total; e += 32)
+        if (sh.spk[0][e] == sh.spk[0][e + 1] &&
+            !ev_less(sh.td[0][e], sh.tgt[0][e], 0, sh.td[0][e + 1], sh.tgt[0][e + 1], 0))
+            sorted = false;
+    sorted = __all_sync(0xffffffffu, sorted);
+    if (sorted && nrun == 1) {
+        for (int e = lane; e < total; e += 32) {
+            sh.td[1][e] = sh.td[0][e];
+            sh.tgt[1][e] = sh.tgt[0][e];
+            sh.spk[1][e] = sh.spk[0][e];
+        }
+    } else if (sorted) {
+        int run = 0;
+        for (int e = lane; e < total; e += 32) {
+            while (e >= sh.rs[run + 1]) ++run;
+            const double te = sh.td[0][e];
+            const int ge = sh.tgt[0][e], se = sh.spk[0][e];
+            int rank = e - sh.rs[run];
+            for (int q = 0; q < nrun; ++q) {
+                if (q == run) continue;
+                int lo = sh.rs[q], hi = sh.rs[q + 1];   // first element of run q not below e
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (ev_less(sh.td[0][mid], sh.tgt[0][mid], sh.spk[0][mid], te, ge, se)) lo = mid + 1;
+                    else hi = mid;
+                }
+                rank += lo - sh.rs[q];
+            }
+            sh.td[1][rank] = te;
+            sh.tgt[1][rank] = ge;
+            sh.spk[1][rank] = se;
+        }
+    } else {
+        for (int e = lane; e < total; e += 32) {
+            const double te = sh.td[0][e];
+            const int ge = sh.tgt[0][e], se = sh.spk[0][e];
+            int rank = 0;
+            for (int f = 0; f < total; ++f) rank += ev_less(sh.td[0][f], sh.tgt[0][f], sh.spk[0][f], te, ge, se);
+            sh.td[1][rank] = te;
+            sh.tgt[1][rank] = ge;
+            sh.spk[1][rank] = se;
+        }
+    }
+    __syncwarp();
+}
+
+// Processes the ranked events of row i, 32 at a time.  An event is delivered
+// at the first step whose time reaches its delivery time.  Events that cannot
+// change the row's state commit in parallel; the first one that can (or a
+// target seen twice in the chunk) goes through g_deliver alone.
+template <class R>
+__device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
+                                          size_t r, int sa, const double* Tseg, int total, const RowShared& sh,
+                                          int lane)
+{
+    const SynParams& sp = g.sp;
+    int base = 0;
+    while (base < total) {
+        const int e = base + lane;
+        const bool has = e < total;
+        const int rem = g.remodeled[r];
+        const int sc = g.sup_cnt[r];
+        const bool sat = sc == sp.Nss;
+        bool changing = false, do_write = false, new_pre = false, is_active = false;
+        double wv = 0.0, w2 = 0.0, td = 0.0;
+        int t = -1, spk = 0, pc = 0, sd = sa;
+        size_t ij = 0;
+        if (has) {
+            td = sh.td[1][e];
+            t = sh.tgt[1][e];
+            spk = sh.spk[1][e];
+            while (Tseg[sd - sa] < td) ++sd;
+            ij = gidx(g, b, i, t);
+            is_active = g.active[ij] == 1;
+            const bool su = g.super[ij] == 1;
+            wv = g.W[ij];
+            pc = g.pre_cnt[ij];
+            if (pc == 0) {
+                new_pre = true;
+            } else {
+                const int last = g.pre_step[ij * kPreRing + ((pc - 1) % kPreRing)];
+                new_pre = td > n.T[last] + g.D[ij] + 30.0;
+            }
+            w2 = wv;
+            if (new_pre && (!sat || su)) {
+                const double now = Tseg[sd - sa];
+                const int np = post_num(g, b, t);
+                for (int k = 0; k < np; ++k) {
+                    const double tp = n.T[post_at(g, b, t, k)];
+                    if (!(tp >= now - 100.0)) continue;
+                    g_LTD(sp, w2, tp - td);
+                    do_write = true;
+                    changing |= (w2 >= sp.ACTIVATION_THRESHOLD && !is_active && rem == 0) ||
+                                (w2 >= sp.SUPERSYNAPSE_THRESHOLD && !su && sc < sp.Nss) ||
+                                (w2 < sp.SUPERSYNAPSE_THRESHOLD && su) ||
+                                (w2 < sp.ACTIVATION_THRESHOLD && is_active);
+                }
+            }
+            const unsigned same = __match_any_sync(__activemask(), t);
+            if (__popc(same) > 1 && lane != __ffs(same) - 1) changing = true;
+        }
+        const unsigned chg = __ballot_sync(0xffffffffu, has && changing);
+        const int nchunk = min(32, total - base);
+        const int f = chg ? __ffs(chg) - 1 : nchunk;
+        if (has && lane < f) {
+            if (is_active) {
+                const size_t slot = (size_t)(n.syncidx[sd] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + t;
+                atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(wv * kFixScale));
+            }
+            if (new_pre) {
+                g.pre_step[ij * kPreRing + (pc % kPreRing)] = (short)spk;
+                if (pc < 252) g.pre_cnt[ij] = (uint8_t)(pc + 1);
+                else atomicOr(g.error, kErrEventCapacity);
+            }
+            if (do_write) g.W[ij] = w2;
+        }
+        __syncwarp();
+        if (f < nchunk) {
+            const int sdf = __shfl_sync(0xffffffffu, sd, f);
+            if (lane == 0) g_deliver(g, n, bt, b, i, sh.tgt[1][base + f], sdf, sh.spk[1][base + f], sh.td[1][base + f]);
+            __syncwarp();
+            base += f + 1;
+        } else {
+            base += nchunk;
+        }
+    }
+}
+
+// Row i's deliveries over steps s0..s1, one warp per row.  The interval is cut
+// at row i's own spikes (a spike opens a stream whose saturated snapshot
+// depends on the deliveries before it).  Within a segment [sa, sb] the
+// reference delivers, step by step, every event due at that step in (time,
+// target) order; since the delivery step rises with the delivery time, that
+// is the (time, target, spike) order of all events due by T[sb], which the
+// warp gathers and ranks once per segment.  A segment whose events overflow
+// the buffer is replayed step by step, and a step that still overflows is
+// drained one event at a time.
 template <class R>
 __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0,
                                                                 int s1)
 {
-    __shared__ double sh_td[kRowWarps][2][kDueCap];
-    __shared__ int sh_t[kRowWarps][2][kDueCap];
-    __shared__ int sh_sp[kRowWarps][2][kDueCap];
-    __shared__ int sh_newc[kRowWarps][kMaxStreams];
+    extern __shared__ __align__(16) unsigned char row_smem[];
+    __shared__ double sh_T[kSegSteps];
     const int b = blockIdx.y;
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k <= s1 - s0 && k < kSegSteps; k += blockDim.x) sh_T[k] = n.T[s0 + k];
+    __syncthreads();
     const int i = blockIdx.x * kRowWarps + w;
     if (i >= g.n) return;
+    if (s1 - s0 >= kSegSteps) {
+        if (lane == 0) atomicOr(g.error, kErrEventCapacity);
+        return;
+    }
+    RowShared& sh = reinterpret_cast<RowShared*>(row_smem)[w];
     const size_t r = (size_t)b * g.n + i;
     const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
     int head = g.st_head[r], num = g.st_num[r];
@@ -309,146 +516,31 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, Net
     int* stT = g.st_tgt + r * kMaxStreams * kMaxNss;
     const int* perm = g.perm + r * (g.n - 1);
     const double* Drow = g.D + r * g.n;
-    const SynParams& sp = g.sp;
-    double* btd = sh_td[w][0];
-    int* bt_t = sh_t[w][0];
-    int* bsp = sh_sp[w][0];
-    double* otd = sh_td[w][1];
-    int* ot = sh_t[w][1];
-    int* osp = sh_sp[w][1];
-    for (int s = s0; s <= s1; ++s) {
-        const double Ts = n.T[s];
-        if ((bits >> (s - s0)) & 1u) {
-            if (lane == 0) num = g_open_stream(g, r, s, Ts, Drow, head, num, stS, stC, stL, stT);
+    int sa = s0;
+    while (sa <= s1) {
+        if ((bits >> (sa - s0)) & 1u) {
+            if (lane == 0) num = g_open_stream(g, r, sa, sh_T[sa - s0], Drow, head, num, stS, stC, stL, stT);
             num = __shfl_sync(0xffffffffu, num, 0);
             __syncwarp();
         }
-        // gather the due events of every stream
-        int total = 0;
-        bool overflow = false;
-        for (int q = 0; q < num && !overflow; ++q) {
-            const int slot = (head + q) % kMaxStreams;
-            const int L = stL[slot];
-            const int len = L < 0 ? -L : L;
-            int c = stC[slot];
-            const int spk = stS[slot];
-            const double Tsp = n.T[spk];
-            while (c < len) {
-                const int idx = c + lane;
-                bool due = false;
-                double td = 0.0;
-                int t = 0;
-                if (idx < len) {
-                    t = L < 0 ? stT[slot * kMaxNss + idx] : perm[idx];
-                    td = Tsp + Drow[t];
-                    due = Ts >= td;
-                }
-                const unsigned m = __ballot_sync(0xffffffffu, due);
-                const int nd = __popc(m);   // delivery times rise along a stream: the due set is a prefix
-                if (total + nd > kDueCap) {
-                    overflow = true;
-                    break;
-                }
-                if (due) {
-                    btd[total + lane] = td;
-                    bt_t[total + lane] = t;
-                    bsp[total + lane] = spk;
-                }
-                total += nd;
-                c += nd;
-                if (nd < 32) break;
-            }
-            if (lane == 0) sh_newc[w][q] = c;
-        }
-        __syncwarp();
-        if (overflow) {
-            // more due events than the buffer holds: the exact one-by-one drain
-            if (lane == 0) g_drain_seq(g, n, bt, b, i, s, Ts, head, num, stS, stC, stL, stT, perm, Drow);
-            __syncwarp();
-        } else if (total > 0) {
-            for (int q = lane; q < num; q += 32) stC[(head + q) % kMaxStreams] = sh_newc[w][q];
-            // rank by (time, target, position): distinct keys, so ranks are a permutation
-            for (int e = lane; e < total; e += 32) {
-                const double te = btd[e];
-                const int ge = bt_t[e];
-                int rank = 0;
-                for (int f = 0; f < total; ++f) {
-                    const double tf = btd[f];
-                    const int gf = bt_t[f];
-                    rank += (tf < te) || (tf == te && (gf < ge || (gf == ge && f < e)));
-                }
-                otd[rank] = te;
-                ot[rank] = ge;
-                osp[rank] = bsp[e];
-            }
-            __syncwarp();
-            int base = 0;
-            while (base < total) {
-                const int e = base + lane;
-                const bool has = e < total;
-                const int rem = g.remodeled[r];
-                const int sc = g.sup_cnt[r];
-                const bool sat = sc == sp.Nss;
-                bool changing = false, do_write = false, new_pre = false, is_active = false;
-                double wv = 0.0, w2 = 0.0, td = 0.0;
-                int t = -1, spk = 0, pc = 0;
-                size_t ij = 0;
-                if (has) {
-                    td = otd[e];
-                    t = ot[e];
-                    spk = osp[e];
-                    ij = gidx(g, b, i, t);
-                    is_active = g.active[ij] == 1;
-                    const bool su = g.super[ij] == 1;
-                    wv = g.W[ij];
-                    pc = g.pre_cnt[ij];
-                    if (pc == 0) {
-                        new_pre = true;
-                    } else {
-                        const int last = g.pre_step[ij * kPreRing + ((pc - 1) % kPreRing)];
-                        new_pre = td > n.T[last] + g.D[ij] + 30.0;
-                    }
-                    w2 = wv;
-                    if (new_pre && (!sat || su)) {
-                        const double now = Ts;
-                        const int np = post_num(g, b, t);
-                        for (int k = 0; k < np; ++k) {
-                            const double tp = n.T[post_at(g, b, t, k)];
-                            if (!(tp >= now - 100.0)) continue;
-                            g_LTD(sp, w2, tp - td);
-                            do_write = true;
-                            changing |= (w2 >= sp.ACTIVATION_THRESHOLD && !is_active && rem == 0) ||
-                                        (w2 >= sp.SUPERSYNAPSE_THRESHOLD && !su && sc < sp.Nss) ||
-                                        (w2 < sp.SUPERSYNAPSE_THRESHOLD && su) ||
-                                        (w2 < sp.ACTIVATION_THRESHOLD && is_active);
-                        }
-                    }
-                    // a target twice in one chunk goes through the exact path
-                    const unsigned same = __match_any_sync(__activemask(), t);
-                    if (__popc(same) > 1 && lane != __ffs(same) - 1) changing = true;
-                }
-                const unsigned chg = __ballot_sync(0xffffffffu, has && changing);
-                const int nchunk = min(32, total - base);
-                const int f = chg ? __ffs(chg) - 1 : nchunk;
-                if (has && lane < f) {
-                    if (is_active) {
-                        const size_t slot = (size_t)(n.syncidx[s] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + t;
-                        atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(wv * kFixScale));
-                    }
-                    if (new_pre) {
-                        g.pre_step[ij * kPreRing + (pc % kPreRing)] = (short)spk;
-                        if (pc < 252) g.pre_cnt[ij] = (uint8_t)(pc + 1);
-                        else atomicOr(g.error, kErrEventCapacity);
-                    }
-                    if (do_write) g.W[ij] = w2;
-                }
-                __syncwarp();
-                if (f < nchunk) {
-                    if (lane == 0) g_deliver(g, n, bt, b, i, ot[base + f], s, osp[base + f], otd[base + f]);
+        const uint32_t later = (sa - s0 + 1) < 32 ? bits >> (sa - s0 + 1) : 0u;
+        const int sb = later ? sa + __ffs(later) - 1 : s1;
+        int nrun = 0;
+        int total = num > 0 ? g_gather(g, n, sh_T[sb - s0], head, num, stS, stC, stL, stT, perm, Drow, sh, lane, nrun)
+                            : 0;
+        if (total > 0) {
+            g_rank(sh, total, nrun, lane);
+            g_process(g, n, bt, b, i, r, sa, sh_T + (sa - s0), total, sh, lane);
+        } else if (total < 0) {
+            for (int s = sa; s <= sb; ++s) {
+                total = g_gather(g, n, sh_T[s - s0], head, num, stS, stC, stL, stT, perm, Drow, sh, lane, nrun);
+                if (total > 0) {
+                    g_rank(sh, total, nrun, lane);
+                    g_process(g, n, bt, b, i, r, s, sh_T + (s - s0), total, sh, lane);
+                } else if (total < 0) {
+                    if (lane == 0)
+                        g_drain_seq(g, n, bt, b, i, s, sh_T[s - s0], head, num, stS, stC, stL, stT, perm, Drow);
                     __syncwarp();
-                    base += f + 1;
-                } else {
-                    base += nchunk;
                 }
             }
         }
@@ -460,6 +552,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, Net
             --num;
         }
         __syncwarp();
+        sa = sb + 1;
     }
     if (lane == 0) {
         g.st_head[r] = head;

@@ -111,7 +111,7 @@ cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const Bat
 {
     const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
     const dim3 wrows((g.n + kRowWarps - 1) / kRowWarps, g.B);
-    UG_TIMED(lc, "k_growth_rows", (k_growth_rows<R><<<wrows, 32 * kRowWarps, 0, lc.main>>>(g, n, b, s0, s1)));
+    UG_TIMED(lc, "k_growth_rows", (k_growth_rows<R><<<wrows, 32 * kRowWarps, kRowWarps * sizeof(RowShared), lc.main>>>(g, n, b, s0, s1)));
     UG_TIMED(lc, "k_growth_newpost", (k_growth_newpost<R><<<g.B, 1024, 0, lc.main>>>(g, n, b, s0, s1)));
     UG_TIMED(lc, "k_growth_ltp", (k_growth_ltp<R><<<rows, kBlock, 0, lc.main>>>(g, n, s1)));
     return cudaGetLastError();
