@@ -127,6 +127,29 @@ ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, 
  * passes true). */
 ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials,
                                int32_t training);
+
+/* One item of a group run. */
+typedef struct {
+    int32_t net;           /* network id */
+    int32_t kind;          /* 0: test trials, 1: growth trials */
+    uint32_t first_trial;  /* trial index of the item's first trial */
+    int32_t n_trials;      /* test: trials run together as one batch; growth: consecutive trials */
+    int32_t training;      /* growth: the training neurons get their kick */
+    int32_t status;        /* out: the item's ug_status */
+} ug_group_item;
+
+/* No counterpart in the reference, whose processes grow one network each.  Runs several
+ * loaded networks together: every kernel launch of a trial steps all of them.  Test items
+ * run their n_trials in the first round as one batch (as ug_run_test_trials); growth items
+ * run one trial per round (as ug_run_growth_trials), and rounds continue until every item
+ * is done.  Each network ends in the state, and gives the results, that the
+ * single-network calls give; read them with the getters.  The networks must share
+ * num_steps and appear once each.  Returns the first failing status (UG_OK if none); the
+ * items' status fields say which failed, and a failed item drops out of later rounds. */
+ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items);
+/* Caps the blocks per SM of the group launches of the two integrators (0: the occupancy
+ * limit).  The autotuner's knob. */
+ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm);
 /* Dense n_ra x n_ra RA->RA weights (weights_RA_RA). */
 ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out);
 /* Dense n_ra x n_ra axonal delays (axonal_delays_RA_RA). */

@@ -67,6 +67,7 @@ struct GrowthDev {
     int* newpost;           // [B][n * 16] new post events of the interval, in order
     int* newpost_cnt;       // [B]
     int* error;
+    int* row_stamp;         // [B][n] interval stamps of the group row queue, or null
 };
 
 __device__ __forceinline__ size_t gidx(const GrowthDev& g, int b, int i, int j)
@@ -489,27 +490,16 @@ __device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n
 // warp gathers and ranks once per segment.  A segment whose events overflow
 // the buffer is replayed step by step, and a step that still overflows is
 // drained one event at a time.
+// One warp, row i of instance b; sh_T holds T[s0..s1].  Returns the row's
+// live streams after the interval.
 template <class R>
-__global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0,
-                                                                int s1)
+__device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
+                                     int s0, int s1, const double* sh_T, RowShared& sh, int lane)
 {
-    extern __shared__ __align__(16) unsigned char row_smem[];
-    __shared__ double sh_T[kSegSteps];
-    const int b = blockIdx.y;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int k = threadIdx.x; k <= s1 - s0 && k < kSegSteps; k += blockDim.x) sh_T[k] = n.T[s0 + k];
-    __syncthreads();
-    const int i = blockIdx.x * kRowWarps + w;
-    if (i >= g.n) return;
-    if (s1 - s0 >= kSegSteps) {
-        if (lane == 0) atomicOr(g.error, kErrEventCapacity);
-        return;
-    }
-    RowShared& sh = reinterpret_cast<RowShared*>(row_smem)[w];
     const size_t r = (size_t)b * g.n + i;
     const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
     int head = g.st_head[r], num = g.st_num[r];
-    if (bits == 0 && num == 0) return;
+    if (bits == 0 && num == 0) return 0;
     int* stS = g.st_step + r * kMaxStreams;
     int* stC = g.st_cursor + r * kMaxStreams;
     int* stL = g.st_len + r * kMaxStreams;
@@ -558,6 +548,26 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, Net
         g.st_head[r] = head;
         g.st_num[r] = num;
     }
+    return num;
+}
+
+template <class R>
+__global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0,
+                                                                int s1)
+{
+    extern __shared__ __align__(16) unsigned char row_smem[];
+    __shared__ double sh_T[kSegSteps];
+    const int b = blockIdx.y;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int k = threadIdx.x; k <= s1 - s0 && k < kSegSteps; k += blockDim.x) sh_T[k] = n.T[s0 + k];
+    __syncthreads();
+    const int i = blockIdx.x * kRowWarps + w;
+    if (i >= g.n) return;
+    if (s1 - s0 >= kSegSteps) {
+        if (lane == 0) atomicOr(g.error, kErrEventCapacity);
+        return;
+    }
+    g_row(g, n, bt, b, i, s0, s1, sh_T, reinterpret_cast<RowShared*>(row_smem)[w], lane);
 }
 
 // New post-synaptic events of the interval in the reference's order: steps
@@ -565,9 +575,9 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, Net
 // post events recorded before this interval; then the sync time is appended
 // to each (:9385-9386).  One block per instance.
 template <class R>
-__global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+__device__ __forceinline__ void g_newpost_body(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int s0,
+                                               int s1)
 {
-    const int b = blockIdx.x;
     __shared__ int cnt;
     __shared__ int wsum[32];
     // most intervals hold no somatic spike at all
@@ -629,13 +639,18 @@ __global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> 
     }
 }
 
+template <class R>
+__global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+{
+    g_newpost_body(g, n, bt, (int)blockIdx.x, s0, s1);
+}
+
 // LTP / LTD of every row against the interval's new post events, then axon
 // remodeling (NetworkGrowthSimulator.cpp:9392-9554).
 template <class R>
-__global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n, int s1)
+__device__ __forceinline__ void g_ltp_body(const GrowthDev& g, const NetDev<R>& n, int s1, int bx, int b)
 {
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = bx * kBlock + threadIdx.x;
     if (i >= g.n) return;
     const int total = g.newpost_cnt[b];
     if (total == 0) return;
@@ -670,12 +685,16 @@ __global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n,
     if (g.sup_cnt[r] == sp.Nss && g.remodeled[r] == 0) g_axon_remodeling(g, b, i);
 }
 
-// potentiation_decay + update_all_synapses (:16346-16361, :16432-16443).
 template <class R>
-__global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
+__global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n, int s1)
 {
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    g_ltp_body(g, n, s1, (int)blockIdx.x, (int)blockIdx.y);
+}
+
+// potentiation_decay + update_all_synapses (:16346-16361, :16432-16443).
+__device__ __forceinline__ void g_epilogue_body(const GrowthDev& g, int bx, int b)
+{
+    const int i = bx * kBlock + threadIdx.x;
     if (i >= g.n) return;
     const SynParams& sp = g.sp;
     double* Wr = g.W + ((size_t)b * g.n + i) * g.n;
@@ -689,20 +708,33 @@ __global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
     for (int j = 0; j < g.n; ++j) g_update_synapse(g, b, i, j);
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
+{
+    g_epilogue_body(g, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // Start of a growth trial: no streams, no pre or post events
 // (the reference's trial-local containers, :8869-8880).
-template <class R>
-__global__ void k_growth_reset(GrowthDev g)
+// Part `part` of `nparts` of the reset, blockDim.x threads per part.
+__device__ __forceinline__ void g_reset_body(const GrowthDev& g, int part, int nparts)
 {
-    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t tid = (size_t)part * blockDim.x + threadIdx.x;
     const size_t nr = (size_t)g.B * g.n;
     const size_t npair = nr * g.n;
-    for (size_t k = tid; k < npair; k += (size_t)gridDim.x * blockDim.x) g.pre_cnt[k] = 0;
-    for (size_t k = tid; k < nr; k += (size_t)gridDim.x * blockDim.x) {
+    for (size_t k = tid; k < npair; k += (size_t)nparts * blockDim.x) g.pre_cnt[k] = 0;
+    for (size_t k = tid; k < nr; k += (size_t)nparts * blockDim.x) {
         g.post_cnt[k] = 0;
         g.st_head[k] = 0;
         g.st_num[k] = 0;
+        if (g.row_stamp) g.row_stamp[k] = 0;
     }
+}
+
+template <class R>
+__global__ void k_growth_reset(GrowthDev g)
+{
+    g_reset_body(g, (int)blockIdx.x, (int)gridDim.x);
 }
 
 // remove_neurons_from_network, NetworkGrowthSimulator.cpp:15757-15859: every
@@ -760,12 +792,17 @@ __global__ void __launch_bounds__(kBlock) k_growth_remove(GrowthDev g, const int
 
 // check_bad_values (HH2_test.cpp:244-260) over every RA neuron of every instance.
 template <class R>
-__global__ void k_check_bad(NetDev<R> n, BatchDev<R> bt, int* bad)
+__device__ __forceinline__ void check_bad_body(const NetDev<R>& n, const BatchDev<R>& bt, int* bad, size_t k)
 {
-    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= (size_t)bt.B * n.n_ra) return;
     const double vs = (double)bt.ra[0][k], vd = (double)bt.ra[1][k];
     if (vs > 100 || vs < -200 || isnan(vs) || vd > 100 || vd < -200 || isnan(vd)) atomicOr(bad, 1);
+}
+
+template <class R>
+__global__ void k_check_bad(NetDev<R> n, BatchDev<R> bt, int* bad)
+{
+    check_bad_body(n, bt, bad, (size_t)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
 }  // namespace ug

@@ -208,6 +208,14 @@ public:
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (ggraph_) cudaGraphExecDestroy(ggraph_);
     }
+    // Group participation (ug_run_group): per-trial preparation, the member
+    // descriptor, and the per-trial tail of a growth trial.
+    ug_status prepare_test(uint32_t first_trial, int n_trials, cudaStream_t st);
+    ug_status prepare_growth(uint32_t trial, int training, cudaStream_t st);
+    ug_status member(ug::GroupMember<R>* m, int index, int2* act_rows, int* act_cnt, int act_cap, bool growth);
+    ug_status finish_growth(uint32_t trial, int bad, cudaStream_t st);
+    ug_status finish_test(cudaStream_t st) { return check_error(st); }
+    size_t growth_row_count() const { return (size_t)h.n_ra; }
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -251,7 +259,7 @@ private:
     ug::GrowthDev gd_{};
     DevMem gW_, gD_, gPerm_, gActive_, gSuper_, gActList_, gActCnt_, gSupList_, gSupCnt_, gRemod_, gPreStep_,
         gPreCnt_, gPostStep_, gPostCnt_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
-        gNewpostCnt_, gSomaBits_, gBad_, gRep_;
+        gNewpostCnt_, gSomaBits_, gBad_, gRep_, gStamp_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
 };
@@ -511,19 +519,7 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
                                       int64_t* launches)
 {
     cudaStream_t st = lc.main;
-    if (n_trials <= 0 || n_trials > 65535) return fail(UG_EINVAL, "n_trials must be in [1, 65535]");
-    if (rara_dirty_) UG_TRY(sync_static_lists(st));
-    UG_TRY(ensure_batch(n_trials));
-    bd_.soma_bits = nullptr;
-    bd_.B = n_trials;
-    bd_.kick_on = 1;
-    bd_.scatter_rara = 1;
-    B_ = n_trials;
-    std::vector<uint32_t> tr(n_trials);
-    std::vector<double> mi(n_trials, kMeanInjectionTest);
-    for (int k = 0; k < n_trials; ++k) tr[k] = first_trial + (uint32_t)k;
-    UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), tr.data(), tr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-    UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), mi.data(), mi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    UG_TRY(prepare_test(first_trial, n_trials, st));
     if (!graphs || lc.timer) return issue_batch(lc, launches);
     if (!graph_exec_ || graph_B_ != n_trials) {
         if (graph_exec_) {
@@ -549,6 +545,26 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
     }
     UG_CUDA(cudaGraphLaunch(graph_exec_, st));
     if (launches) *launches += 2 * ((int64_t)sync_steps.size() + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::prepare_test(uint32_t first_trial, int n_trials, cudaStream_t st)
+{
+    if (n_trials <= 0 || n_trials > 65535) return fail(UG_EINVAL, "n_trials must be in [1, 65535]");
+    if (rara_dirty_) UG_TRY(sync_static_lists(st));
+    UG_TRY(ensure_batch(n_trials));
+    bd_.soma_bits = nullptr;
+    bd_.B = n_trials;
+    bd_.kick_on = 1;
+    bd_.scatter_rara = 1;
+    B_ = n_trials;
+    std::vector<uint32_t> tr(n_trials);
+    std::vector<double> mi(n_trials, kMeanInjectionTest);
+    for (int k = 0; k < n_trials; ++k) tr[k] = first_trial + (uint32_t)k;
+    UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), tr.data(), tr.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), mi.data(), mi.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaStreamSynchronize(st));
     return UG_OK;
 }
 
@@ -736,20 +752,9 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
 {
     cudaStream_t st = lc.main;
     if (n_trials <= 0) return fail(UG_EINVAL, "n_trials must be positive");
-    if (!growth_ready_) UG_TRY(growth_init(st));
-    UG_TRY(ensure_batch(1));
-    bd_.B = 1;
-    bd_.kick_on = training ? 1 : 0;
-    bd_.scatter_rara = 0;
-    bd_.soma_bits = gSomaBits_.as<int>();
-    B_ = 1;
     for (int t = 0; t < n_trials; ++t) {
         const uint32_t trial = first_trial + (uint32_t)t;
-        // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
-        ug::HostStream hs{ug::make_stream(h.seed, ug::kNoiseTrial, (uint32_t)h.net_id, 0, trial), 0};
-        const double mean_inj = 100.0 + ug::random_G(300.0, hs.word());
-        UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), &trial, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-        UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), &mean_inj, sizeof(double), cudaMemcpyHostToDevice, st));
+        UG_TRY(prepare_growth(trial, training, st));
         if (!graphs || lc.timer) {
             UG_TRY(issue_growth_trial(lc, launches));
         } else {
@@ -785,10 +790,64 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
         UG_CUDA(ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), st));
         int bad = 0;
         UG_CUDA(cudaMemcpyAsync(&bad, gBad_.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, st));
-        UG_TRY(check_error(st));
-        if (bad) return fail(UG_ENUMERIC, "bad values in the neuron dynamics (check_bad_values)");
-        rara_dirty_ = true;
-        UG_TRY(after_growth_trial(trial, st));
+        UG_TRY(finish_growth(trial, bad, st));
+    }
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::prepare_growth(uint32_t trial, int training, cudaStream_t st)
+{
+    if (!growth_ready_) UG_TRY(growth_init(st));
+    UG_TRY(ensure_batch(1));
+    bd_.B = 1;
+    bd_.kick_on = training ? 1 : 0;
+    bd_.scatter_rara = 0;
+    bd_.soma_bits = gSomaBits_.as<int>();
+    B_ = 1;
+    // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
+    ug::HostStream hs{ug::make_stream(h.seed, ug::kNoiseTrial, (uint32_t)h.net_id, 0, trial), 0};
+    const double mean_inj = 100.0 + ug::random_G(300.0, hs.word());
+    UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), &trial, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), &mean_inj, sizeof(double), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+// bad: the check_bad_values flag of the trial (read back by the caller's stream).
+template <class R>
+ug_status NetImpl<R>::finish_growth(uint32_t trial, int bad, cudaStream_t st)
+{
+    UG_TRY(check_error(st));
+    if (bad) return fail(UG_ENUMERIC, "bad values in the neuron dynamics (check_bad_values)");
+    rara_dirty_ = true;
+    return after_growth_trial(trial, st);
+}
+
+// Descriptor of this network as member `index` of a group.  Growth members
+// carry the group's row queue; the network's own descriptors, which its
+// single-network graphs were captured with, are left as they are.
+template <class R>
+ug_status NetImpl<R>::member(ug::GroupMember<R>* m, int index, int2* act_rows, int* act_cnt, int act_cap, bool growth)
+{
+    std::memset((void*)m, 0, sizeof(*m));
+    m->n = nd_;
+    m->bt = bd_;
+    m->rc = rc_;
+    m->ic = ic_;
+    m->bt.member = index;
+    m->bt.act_rows = nullptr;
+    m->bt.act_cnt = nullptr;
+    m->bt.row_stamp = nullptr;
+    m->growth = growth ? 1 : 0;
+    if (growth) {
+        if (!gStamp_.as<int>() || gStamp_.bytes() < (size_t)h.n_ra * sizeof(int)) UG_TRY(gStamp_.alloc((size_t)h.n_ra * sizeof(int)));
+        m->g = gd_;
+        m->g.row_stamp = gStamp_.as<int>();
+        m->bt.act_rows = act_rows;
+        m->bt.act_cnt = act_cnt;
+        m->bt.act_cap = act_cap;
+        m->bt.row_stamp = gStamp_.as<int>();
     }
     return UG_OK;
 }
@@ -1035,6 +1094,203 @@ ug_status NetImpl<R>::neuron_props(double* rest, double* gca, int32_t* mature, d
     return UG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Groups: several networks stepped by the same launches (ug_group.cuh).
+
+struct GroupBase {
+    virtual ~GroupBase() = default;
+};
+
+template <class R>
+struct RoundItem {
+    NetImpl<R>* net;
+    int kind;            // 0 test, 1 growth
+    uint32_t trial;      // first trial of this round
+    int n_trials;        // test: batch size
+    int training;
+    ug_status status;
+};
+
+template <class R>
+class GroupExec : public GroupBase {
+public:
+    ~GroupExec() override { drop_graphs(); }
+    ug_status run_round(std::vector<RoundItem<R>>& items, const ug::LaunchCtx& lc, bool graphs, int ra_bps,
+                        int i_bps, int64_t* launches);
+
+private:
+    void drop_graphs()
+    {
+        for (cudaGraphExec_t& g : graph_)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
+    }
+    ug_status reserve(DevMem& m, size_t bytes)
+    {
+        if (m.as<void>() && m.bytes() >= bytes) return UG_OK;
+        drop_graphs();   // the graphs hold the old addresses
+        return m.alloc(std::max<size_t>(bytes * 3 / 2, 256));
+    }
+
+    DevMem members_, items_[ug::kNumLists], count_, act_rows_, act_cnt_, bad_, T_;
+    std::vector<ug::GroupMember<R>> hmem_;
+    std::vector<int4> hitems_[ug::kNumLists];
+    std::vector<int> hcount_, hbad_;
+    std::vector<double> T;
+    std::vector<int> sync_steps;
+    int num_steps_ = -1;
+    int ra_bps_ = -1, i_bps_ = -1;
+    ug::GroupDev dev_{};
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // [with growth members]
+};
+
+template <class R>
+ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::LaunchCtx& lc, bool graphs,
+                                  int ra_bps, int i_bps, int64_t* launches)
+{
+    cudaStream_t st = lc.main;
+    if (items.empty()) return UG_OK;
+    const int num_steps = items[0].net->h.num_steps;
+    for (const RoundItem<R>& it : items)
+        if (it.net->h.num_steps != num_steps)
+            return fail(UG_EINVAL, "the networks of a group must share num_steps (one time grid)");
+    for (size_t a = 0; a < items.size(); ++a)
+        for (size_t b = a + 1; b < items.size(); ++b)
+            if (items[a].net == items[b].net) return fail(UG_EINVAL, "a network appears twice in one group");
+    if (num_steps != num_steps_) {
+        std::vector<int> syncidx;
+        build_schedule(num_steps, T, sync_steps, syncidx);
+        for (size_t q = 0; q < sync_steps.size(); ++q) {
+            const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
+            if (sync_steps[q] - s0 >= ug::kSegSteps) return fail(UG_EINVAL, "sync interval longer than the row kernel handles");
+        }
+        UG_TRY(reserve(T_, T.size() * sizeof(double)));
+        UG_CUDA(cudaMemcpyAsync(T_.as<double>(), T.data(), T.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        num_steps_ = num_steps;
+        drop_graphs();
+    }
+    if (ra_bps != ra_bps_ || i_bps != i_bps_) {
+        UG_CUDA(ug::group_grids<R>(dev_, ra_bps, i_bps));
+        ra_bps_ = ra_bps;
+        i_bps_ = i_bps;
+        drop_graphs();
+    }
+    // per-member preparation (uploads of trial indices and injection times)
+    for (RoundItem<R>& it : items) {
+        it.status = it.kind == 1 ? it.net->prepare_growth(it.trial, it.training, st)
+                                 : it.net->prepare_test(it.trial, it.n_trials, st);
+        if (it.status != UG_OK) return it.status;
+    }
+    // row queue: every row of every growth member at most once per interval
+    bool growth = false;
+    size_t rows = 0;
+    for (const RoundItem<R>& it : items)
+        if (it.kind == 1) {
+            growth = true;
+            rows += it.net->growth_row_count();
+        }
+    UG_TRY(reserve(act_rows_, 2 * std::max<size_t>(rows, 1) * sizeof(int2)));
+    // the capacity (not the current row count) is the kernels' bound, so the
+    // captured graphs stay valid until the buffer grows
+    const int act_cap = (int)(act_rows_.bytes() / (2 * sizeof(int2)));
+    UG_TRY(reserve(act_cnt_, 2 * sizeof(int)));
+    UG_TRY(reserve(bad_, items.size() * sizeof(int)));
+    UG_TRY(reserve(count_, ug::kNumLists * sizeof(int)));
+    // member table and work lists
+    const int M = (int)items.size();
+    hmem_.assign(M, ug::GroupMember<R>());
+    for (auto& v : hitems_) v.clear();
+    for (int m = 0; m < M; ++m) {
+        RoundItem<R>& it = items[m];
+        UG_TRY(it.net->member(&hmem_[m], m, act_rows_.as<int2>(), act_cnt_.as<int>(), act_cap, it.kind == 1));
+        const ug::GroupMember<R>& d = hmem_[m];
+        const int B = d.bt.B, nra = d.n.n_ra, ni = d.n.n_i;
+        const int kb = ug::kBlock;
+        const int nb_ra = (nra + kb - 1) / kb, nb_i = (ni + kb - 1) / kb;
+        const int nb_int = sizeof(R) == 4 ? ((nra + 1) / 2 + kb - 1) / kb : nb_ra;
+        for (int b = 0; b < B; ++b) {
+            for (int x = 0; x < nb_ra + nb_i; ++x) hitems_[ug::kListInit].push_back(make_int4(m, x, b, 0));
+            for (int x = 0; x < nb_int; ++x) hitems_[ug::kListRA].push_back(make_int4(m, x, b, 0));
+            for (int x = 0; x < nb_i; ++x) {
+                hitems_[ug::kListI].push_back(make_int4(m, x, b, 0));
+                if (sizeof(R) == 4) hitems_[ug::kListNoise].push_back(make_int4(m, x, b, 0));
+            }
+        }
+        const int nchk = (int)(((size_t)B * nra + 255) / 256);
+        for (int x = 0; x < nchk; ++x) hitems_[ug::kListCheck].push_back(make_int4(m, x, 0, 0));
+        if (it.kind == 1) {
+            const size_t npair = (size_t)B * nra * nra;
+            const int parts = (int)std::min<size_t>(1024, std::max<size_t>(1, (npair + 256 * 32 - 1) / (256 * 32)));
+            for (int x = 0; x < parts; ++x) hitems_[ug::kListReset].push_back(make_int4(m, x, parts, 0));
+            for (int b = 0; b < B; ++b) {
+                hitems_[ug::kListNewpost].push_back(make_int4(m, 0, b, 0));
+                for (int x = 0; x < nb_ra; ++x) hitems_[ug::kListLtp].push_back(make_int4(m, x, b, 0));
+            }
+        }
+    }
+    UG_TRY(reserve(members_, (size_t)M * sizeof(ug::GroupMember<R>)));
+    UG_CUDA(cudaMemcpyAsync(members_.as<void>(), hmem_.data(), (size_t)M * sizeof(ug::GroupMember<R>),
+                            cudaMemcpyHostToDevice, st));
+    hcount_.assign(ug::kNumLists, 0);
+    for (int k = 0; k < ug::kNumLists; ++k) {
+        hcount_[k] = (int)hitems_[k].size();
+        UG_TRY(reserve(items_[k], std::max<size_t>(hitems_[k].size(), 1) * sizeof(int4)));
+        if (!hitems_[k].empty())
+            UG_CUDA(cudaMemcpyAsync(items_[k].as<int4>(), hitems_[k].data(), hitems_[k].size() * sizeof(int4),
+                                    cudaMemcpyHostToDevice, st));
+    }
+    UG_CUDA(cudaMemcpyAsync(count_.as<int>(), hcount_.data(), ug::kNumLists * sizeof(int), cudaMemcpyHostToDevice, st));
+    UG_CUDA(cudaMemsetAsync(bad_.as<int>(), 0, (size_t)M * sizeof(int), st));
+    dev_.members = members_.as<void>();
+    for (int k = 0; k < ug::kNumLists; ++k) dev_.items[k] = items_[k].as<int4>();
+    dev_.count = count_.as<int>();
+    dev_.act_rows = act_rows_.as<int2>();
+    dev_.act_cnt = act_cnt_.as<int>();
+    dev_.act_cap = act_cap;
+    dev_.bad = bad_.as<int>();
+    dev_.T = T_.as<double>();
+    // launch: one captured graph per kind (with or without growth members),
+    // reused across compositions
+    const int64_t Q = (int64_t)sync_steps.size();
+    const int64_t n_launch = 2 + (sizeof(R) == 4 ? 1 : 0) + 2 * (Q + 1) + (growth ? 3 * Q + 2 : 0);
+    if (!graphs || lc.timer) {
+        UG_CUDA(ug::launch_group_trial<R>(dev_, sync_steps, num_steps, growth, lc, nullptr));
+    } else {
+        cudaGraphExec_t& ge = graph_[growth ? 1 : 0];
+        if (!ge) {
+            cudaStream_t cap;
+            UG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            cudaGraph_t g;
+            UG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+            ug::LaunchCtx clc = lc;
+            clc.main = cap;
+            int64_t dummy = 0;
+            cudaError_t e = ug::launch_group_trial<R>(dev_, sync_steps, num_steps, growth, clc, &dummy);
+            cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+            cudaStreamDestroy(cap);
+            UG_CUDA(e);
+            UG_CUDA(e2);
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            UG_CUDA(e);
+        }
+        UG_CUDA(cudaGraphLaunch(ge, st));
+    }
+    if (launches) *launches += n_launch;
+    hbad_.assign(M, 0);
+    UG_CUDA(cudaMemcpyAsync(hbad_.data(), bad_.as<int>(), (size_t)M * sizeof(int), cudaMemcpyDeviceToHost, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    ug_status first = UG_OK;
+    for (int m = 0; m < M; ++m) {
+        RoundItem<R>& it = items[m];
+        it.status = it.kind == 1 ? it.net->finish_growth(it.trial, hbad_[m], st) : it.net->finish_test(st);
+        if (it.status != UG_OK && first == UG_OK) first = it.status;
+    }
+    return first;
+}
+
 }  // namespace
 
 struct ug_ctx {
@@ -1060,6 +1316,8 @@ struct ug_ctx {
     int64_t launches = 0;
     int next_id = 0;
     std::map<int, std::unique_ptr<NetBase>> nets;
+    std::unique_ptr<GroupBase> group;          // GroupExec<float> or GroupExec<double>
+    int group_ra_bps = 0, group_i_bps = 0;     // integrator blocks per SM of group launches (0: occupancy)
 };
 
 namespace {
@@ -1073,6 +1331,58 @@ ug_status get_net(ug_ctx* c, int id, NetBase** out)
     return UG_OK;
 }
 
+}  // namespace
+
+namespace {
+template <class R>
+ug_status run_group_typed(ug_ctx* ctx, ug_group_item* items, int n_items)
+{
+    if (!ctx->group) ctx->group.reset(new GroupExec<R>());
+    GroupExec<R>* ge = static_cast<GroupExec<R>*>(ctx->group.get());
+    std::vector<NetImpl<R>*> nets(n_items);
+    int rounds = 0;
+    for (int k = 0; k < n_items; ++k) {
+        NetBase* nb;
+        UG_TRY(get_net(ctx, items[k].net, &nb));
+        nets[k] = static_cast<NetImpl<R>*>(nb);
+        if (items[k].kind != 0 && items[k].kind != 1) return fail(UG_EINVAL, "group item kind must be 0 or 1");
+        if (items[k].n_trials <= 0) return fail(UG_EINVAL, "group item n_trials must be positive");
+        items[k].status = UG_OK;
+        rounds = std::max(rounds, items[k].kind == 1 ? items[k].n_trials : 1);
+    }
+    ug_status first = UG_OK;
+    for (int r = 0; r < rounds; ++r) {
+        std::vector<RoundItem<R>> round;
+        std::vector<int> idx;
+        for (int k = 0; k < n_items; ++k) {
+            const ug_group_item& it = items[k];
+            if (it.status != UG_OK) continue;
+            if (it.kind == 0 && r == 0)
+                round.push_back({nets[k], 0, it.first_trial, it.n_trials, 1, UG_OK});
+            else if (it.kind == 1 && r < it.n_trials)
+                round.push_back({nets[k], 1, it.first_trial + (uint32_t)r, 1, it.training, UG_OK});
+            else
+                continue;
+            idx.push_back(k);
+        }
+        if (round.empty()) break;
+        const ug_status s = ge->run_round(round, ctx->launch_ctx(), ctx->graphs, ctx->group_ra_bps,
+                                          ctx->group_i_bps, &ctx->launches);
+        bool attributed = false;
+        for (size_t j = 0; j < round.size(); ++j) {
+            items[idx[j]].status = round[j].status;
+            attributed |= round[j].status != UG_OK;
+        }
+        if (s != UG_OK) {
+            if (first == UG_OK) first = s;
+            if (!attributed) {   // the round itself failed: no member finished it
+                for (int k : idx) items[k].status = s;
+                break;
+            }
+        }
+    }
+    return first;
+}
 }  // namespace
 
 extern "C" {
@@ -1110,6 +1420,7 @@ void ug_destroy(ug_ctx* ctx)
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamSynchronize(ctx->side);
+    ctx->group.reset();
     ctx->nets.clear();
     ctx->timer.clear(true);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
@@ -1179,6 +1490,26 @@ ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaSetDevice(ctx->device));
     return n->run_growth_trials(first_trial, n_trials, training, ctx->launch_ctx(), ctx->graphs, &ctx->launches);
+}
+
+
+ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    if (n_items < 0 || (n_items > 0 && !items)) return fail(UG_EINVAL, "bad group item array");
+    if (n_items == 0) return UG_OK;
+    UG_CUDA(cudaSetDevice(ctx->device));
+    return ctx->precision == 64 ? run_group_typed<double>(ctx, items, n_items)
+                                : run_group_typed<float>(ctx, items, n_items);
+}
+
+ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    if (ra_blocks_per_sm < 0 || i_blocks_per_sm < 0) return fail(UG_EINVAL, "blocks per SM must be >= 0");
+    ctx->group_ra_bps = ra_blocks_per_sm;
+    ctx->group_i_bps = i_blocks_per_sm;
+    return UG_OK;
 }
 
 ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out)

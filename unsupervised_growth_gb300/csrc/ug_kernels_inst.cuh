@@ -141,4 +141,97 @@ cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad,
     return cudaGetLastError();
 }
 
+template <class K>
+static int occupancy(K kernel, int threads, size_t smem)
+{
+    int nb = 0, dev = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, smem) != cudaSuccess) return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return nb * sms;
+}
+
+template <class R>
+cudaError_t group_grids(GroupDev& d, int ra_blocks_per_sm, int i_blocks_per_sm)
+{
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    d.grid[kListInit] = occupancy(kl_trial_init<R>, kBlock, 0);
+    d.grid[kListNoise] = occupancy(kl_noise_events<R>, kBlock, 0);
+    d.grid[kListRA] = occupancy(kl_interval_ra<R>, kBlock, 0);
+    d.grid[kListI] = occupancy(kl_interval_i<R>, kBlock, 0);
+    if (ra_blocks_per_sm > 0) d.grid[kListRA] = std::min(d.grid[kListRA], ra_blocks_per_sm * sms);
+    if (i_blocks_per_sm > 0) d.grid[kListI] = std::min(d.grid[kListI], i_blocks_per_sm * sms);
+    d.grid[kListReset] = occupancy(kl_growth_reset<R>, 256, 0);
+    d.grid[kListNewpost] = occupancy(kl_growth_newpost<R>, 1024, 0);
+    d.grid[kListLtp] = occupancy(kl_growth_ltp<R>, kBlock, 0);
+    d.grid[kListCheck] = occupancy(kl_check_bad<R>, 256, 0);
+    d.grid[kNumLists] = occupancy(kl_growth_rows<R>, 32 * kRowWarps, kRowWarps * sizeof(RowShared));
+    for (int k = 0; k <= kNumLists; ++k)
+        if (d.grid[k] <= 0) return cudaErrorInvalidConfiguration;
+    return cudaSuccess;
+}
+
+template <class R>
+cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_steps, int num_steps, bool growth,
+                               const LaunchCtx& lc, int64_t* launches)
+{
+    typedef GroupMember<R> M;
+    const M* mem = static_cast<const M*>(d.members);
+    const int* c = d.count;
+    int64_t cnt = 0;
+    cudaError_t e = cudaSuccess;
+    if (growth) {
+        e = cudaMemsetAsync(d.act_cnt, 0, 2 * sizeof(int), lc.main);
+        if (e != cudaSuccess) return e;
+    }
+    UG_TIMED(lc, "k_trial_init", (kl_trial_init<R><<<d.grid[kListInit], kBlock, 0, lc.main>>>(mem, d.items[kListInit], c + kListInit)));
+    ++cnt;
+    if constexpr (sizeof(R) == 4) {
+        UG_TIMED(lc, "k_noise_events", (kl_noise_events<R><<<d.grid[kListNoise], kBlock, 0, lc.main>>>(mem, d.items[kListNoise], c + kListNoise)));
+        ++cnt;
+    }
+    if (growth) {
+        UG_TIMED(lc, "k_growth_reset", (kl_growth_reset<R><<<d.grid[kListReset], 256, 0, lc.main>>>(mem, d.items[kListReset], c + kListReset)));
+        ++cnt;
+    }
+    const bool fork = !lc.timer && lc.side && lc.side != lc.main;
+    const int Q = (int)sync_steps.size();
+    for (int q = 0; q <= Q; ++q) {
+        const int s0 = q == 0 ? 1 : (q < Q ? sync_steps[q - 1] + 1 : num_steps);
+        const int s1 = q < Q ? sync_steps[q] : num_steps - 1;
+        if (fork) {
+            e = cudaEventRecord(lc.fork, lc.main);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.side, lc.fork, 0);
+            if (e != cudaSuccess) return e;
+        }
+        UG_TIMED(lc, "k_interval_ra", (kl_interval_ra<R><<<d.grid[kListRA], kBlock, 0, lc.main>>>(mem, d.items[kListRA], c + kListRA, growth ? d.act_cnt : nullptr, q, s0, s1)));
+        if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
+        kl_interval_i<R><<<d.grid[kListI], kBlock, 0, fork ? lc.side : lc.main>>>(mem, d.items[kListI], c + kListI, q, s0, s1);
+        if (lc.timer) lc.timer->end(lc.main);
+        cnt += 2;
+        if (fork) {
+            e = cudaEventRecord(lc.join, lc.side);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.main, lc.join, 0);
+            if (e != cudaSuccess) return e;
+        }
+        if (growth && q < Q) {
+            UG_TIMED(lc, "k_growth_rows", (kl_growth_rows<R><<<d.grid[kNumLists], 32 * kRowWarps, kRowWarps * sizeof(RowShared), lc.main>>>(mem, d.act_rows, d.act_cnt, d.act_cap, d.T, q, s0, s1)));
+            UG_TIMED(lc, "k_growth_newpost", (kl_growth_newpost<R><<<d.grid[kListNewpost], 1024, 0, lc.main>>>(mem, d.items[kListNewpost], c + kListNewpost, s0, s1)));
+            UG_TIMED(lc, "k_growth_ltp", (kl_growth_ltp<R><<<d.grid[kListLtp], kBlock, 0, lc.main>>>(mem, d.items[kListLtp], c + kListLtp, s1)));
+            cnt += 3;
+        }
+    }
+    if (growth) {
+        UG_TIMED(lc, "k_growth_epilogue", (kl_growth_epilogue<R><<<d.grid[kListLtp], kBlock, 0, lc.main>>>(mem, d.items[kListLtp], c + kListLtp)));
+        ++cnt;
+    }
+    UG_TIMED(lc, "k_check_bad", (kl_check_bad<R><<<d.grid[kListCheck], 256, 0, lc.main>>>(mem, d.items[kListCheck], c + kListCheck, d.bad)));
+    ++cnt;
+    if (launches) *launches += cnt;
+    return cudaGetLastError();
+}
+
 }  // namespace ug

@@ -4,11 +4,12 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <map>
 #include <string>
 #include <vector>
 
-#include "ug_growth.cuh"
+#include "ug_group.cuh"
 
 namespace ug {
 
@@ -112,5 +113,30 @@ template <class R>
 cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st);
 template <class R>
 cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad, cudaStream_t st);
+
+// Group launches (ug_group.cuh): the work lists and row queue of a group, in
+// device memory, and the fixed grid of each list kernel.
+enum GroupList { kListInit = 0, kListNoise, kListRA, kListI, kListReset, kListNewpost, kListLtp, kListCheck, kNumLists };
+struct GroupDev {
+    const void* members = nullptr;            // GroupMember<R>[members]
+    const int4* items[kNumLists] = {};
+    const int* count = nullptr;               // [kNumLists] items in each list
+    int2* act_rows = nullptr;                 // [2][act_cap] row queue
+    int* act_cnt = nullptr;                   // [2]
+    int act_cap = 0;
+    int* bad = nullptr;                       // [members] check_bad_values flags
+    const double* T = nullptr;                // the group's time grid
+    int grid[kNumLists + 1] = {};             // blocks of each list kernel; [kNumLists] = row kernel
+};
+
+// Occupancy-sized grids of the list kernels (call outside stream capture);
+// ra_blocks_per_sm / i_blocks_per_sm > 0 cap the integrators' grids.
+template <class R>
+cudaError_t group_grids(GroupDev& d, int ra_blocks_per_sm, int i_blocks_per_sm);
+// One whole trial of every member: init, the intervals closed by sync_steps,
+// the final empty interval, and, with growth members, the STDP kernels.
+template <class R>
+cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_steps, int num_steps, bool growth,
+                               const LaunchCtx& lc, int64_t* launches);
 
 }  // namespace ug

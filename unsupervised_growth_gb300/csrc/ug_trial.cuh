@@ -85,7 +85,26 @@ struct BatchDev {
     int* error;                // device error bits
     int scatter_rara;          // deliver over the static RA->RA lists (test trial)
     int* soma_bits;            // [B][n_ra] soma-spike step bits of the interval (growth), or null
+    // Group growth: rows that have deliveries to make in an interval (rows that
+    // spiked in it, and rows whose earlier spikes still have events pending).
+    int2* act_rows;            // [2][act_cap] (member, row) lists by interval parity, or null
+    int* act_cnt;              // [2]
+    int act_cap;
+    int member;                // index of this batch in its group
+    int* row_stamp;            // [B][n_ra] 1 + the last interval the row was queued for
 };
+
+// Queues row x of a group growth member for interval q (once per interval).
+template <class R>
+__device__ __forceinline__ void queue_row(const BatchDev<R>& bt, int q, int x)
+{
+    const int tag = q + 1;
+    if (atomicMax(&bt.row_stamp[x], tag) < tag) {
+        const int pos = atomicAdd(&bt.act_cnt[q & 1], 1);
+        if (pos < bt.act_cap) bt.act_rows[(size_t)(q & 1) * bt.act_cap + pos] = make_int2(bt.member, x);
+        else atomicOr(bt.error, kErrEventCapacity);
+    }
+}
 
 // First step s' >= s with T[s'] >= T[s] + d, or num_steps if the trial ends first.
 __device__ __forceinline__ int deliver_step(const double* T, int num_steps, int s, double d)
@@ -242,12 +261,11 @@ __device__ __forceinline__ int i_noise_event(const double* T, int num_steps, int
 // (HH2_test::set_to_rest HH2_test.cpp:191-242, HHI_buffer::set_to_rest
 // HHI_buffer.cpp:178-200, which redraws the interneuron noise times).
 template <class R>
-__global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> bt)
+__device__ __forceinline__ void trial_init_body(const NetDev<R>& n, const BatchDev<R>& bt, int bx, int b)
 {
-    const int b = blockIdx.y;
     const int nb_ra = (n.n_ra + kBlock - 1) / kBlock;
-    if ((int)blockIdx.x < nb_ra) {
-        const int i = blockIdx.x * kBlock + threadIdx.x;
+    if (bx < nb_ra) {
+        const int i = bx * kBlock + threadIdx.x;
         if (i >= n.n_ra) return;
         const size_t x = (size_t)b * n.n_ra + i;
         const R rest[10] = {R(-79.97619025), R(-79.97268759), R(0.01101284), R(0.9932845), R(0.0),
@@ -275,7 +293,7 @@ __global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> 
         }
         if (i == 0) bt.spk_count[b] = 0;
     } else {
-        const int i = (blockIdx.x - nb_ra) * kBlock + threadIdx.x;
+        const int i = (bx - nb_ra) * kBlock + threadIdx.x;
         if (i >= n.n_i) return;
         const size_t x = (size_t)b * n.n_i + i;
         const R rest[7] = {R(-66), R(0.125), R(0.0), R(0.99), R(0.0), R(0), R(0)};
@@ -296,16 +314,21 @@ __global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> 
     }
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> bt)
+{
+    trial_init_body(n, bt, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // HVC(RA) part of one interval: integrates steps s0..s1 (the interval closed
 // by sync q) for every RA neuron of every instance, then scatters the RA->I
 // kicks (and, in test trials, the RA->RA kicks over the static active lists)
 // of the interval's somatic spikes.
 template <class R>
-__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
-                                                        RAStep<R> rc)
+__device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
+                                                 const RAStep<R>& rc, int bx, int b)
 {
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = bx * kBlock + threadIdx.x;
     const bool valid = i < n.n_ra;
     uint32_t soma = 0, dend = 0;
     if (valid) {
@@ -353,6 +376,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(
             }
         }
         if (bt.soma_bits) bt.soma_bits[x] = (int)soma;
+        if (soma && bt.act_rows) queue_row(bt, q, (int)x);
     }
     scatter_warp(soma, i, s0, n.T, n.num_steps, n.syncidx, n.ring, n.ra2i_off, n.ra2i_tgt, n.ra2i_wq, n.ra2i_d,
                  bt.ring_i_exc, (size_t)bt.B * n.n_i, (size_t)b * n.n_i);
@@ -361,16 +385,22 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(
                      bt.ring_ra_exc, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
+                                                                               RAStep<R> rc)
+{
+    interval_ra_body(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // Single-precision HVC(RA) part of one interval, two neurons per thread
 // (neurons 2t and 2t+1) so that every floating-point instruction of the
 // integrator is a packed f32x2 operation.
 template <class R>
-__global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
-                                                           RAStep<R> rc)
+__device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
+                                                    const RAStep<R>& rc, int bx, int b)
 {
     static_assert(sizeof(R) == 4, "the packed RA kernel is single precision");
-    const int b = blockIdx.y;
-    const int t = blockIdx.x * kBlock + threadIdx.x;
+    const int t = bx * kBlock + threadIdx.x;
     const int i0 = 2 * t, i1 = 2 * t + 1;
     const bool v0 = i0 < n.n_ra, v1 = i1 < n.n_ra;
     uint32_t soma0 = 0, dend0 = 0, soma1 = 0, dend1 = 0;
@@ -458,6 +488,7 @@ __global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(Net
                 record_spikes(bt.spk_count, bt.spk_buf, bt.spk_cap, bt.error, b, i, kSpikeDend, de, s0);
             }
             if (bt.soma_bits && (k == 0 || v1)) bt.soma_bits[x] = (int)so;
+            if (so && bt.act_rows) queue_row(bt, q, (int)x);
         }
     }
     for (int k = 0; k < 2; ++k) {
@@ -471,16 +502,22 @@ __global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(Net
     }
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(NetDev<R> n, BatchDev<R> bt, int q, int s0,
+                                                                           int s1, RAStep<R> rc)
+{
+    interval_ra_x2_body(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // Single build: draws every Poisson noise event of the trial for each
 // interneuron of each instance (HHI_buffer::noise_check, HHI_buffer.cpp:278-294,
 // called as exc then inh every step, HHI_buffer.cpp:248-258).  Runs once per
 // batch after k_trial_init; the double-precision work of the noise lives here.
 template <class R>
-__global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R> bt)
+__device__ __forceinline__ void noise_events_body(const NetDev<R>& n, const BatchDev<R>& bt, int bx, int b)
 {
     static_assert(sizeof(R) == 4, "the noise pre-pass serves the single-precision build");
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = bx * kBlock + threadIdx.x;
     if (i >= n.n_i) return;
     const size_t x = (size_t)b * n.n_i + i;
     const StreamId sid = make_stream(n.seed, kNoiseIPoisson, n.net_id, (uint32_t)i, bt.trial[b]);
@@ -514,14 +551,20 @@ __global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R
     bt.i_ev_idx[2 * x + 1] = 0;
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R> bt)
+{
+    noise_events_body(n, bt, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // Single-precision HVC(I) part of one interval: noise kicks from the pre-drawn
 // events, DP8 in the layout of ug_i_f32.cuh.
 template <class R>
-__global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1, IStep<R> ic)
+__device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
+                                                  const IStep<R>& ic, int bx, int b)
 {
     static_assert(sizeof(R) == 4, "single-precision interneuron kernel");
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = bx * kBlock + threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
@@ -569,12 +612,19 @@ __global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev
                  n.i2ra_d, bt.ring_ra_inh, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
 }
 
+template <class R>
+__global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
+                                                                         IStep<R> ic)
+{
+    interval_i_x_body(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
+}
+
 // HVC(I) part of one interval; scatters the I->RA kicks of its spikes.
 template <class R>
-__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_i(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1, IStep<R> ic)
+__device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
+                                                const IStep<R>& ic, int bx, int b)
 {
-    const int b = blockIdx.y;
-    const int i = blockIdx.x * kBlock + threadIdx.x;
+    const int i = bx * kBlock + threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
@@ -619,6 +669,13 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_i(N
     }
     scatter_warp(fired_bits, i, s0, n.T, n.num_steps, n.syncidx, n.ring, n.i2ra_off, n.i2ra_tgt, n.i2ra_wq,
                  n.i2ra_d, bt.ring_ra_inh, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
+}
+
+template <class R>
+__global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_i(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
+                                                                              IStep<R> ic)
+{
+    interval_i_body(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 }  // namespace ug

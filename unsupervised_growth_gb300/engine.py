@@ -23,7 +23,8 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
-            "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_get_weights", "ug_get_delays",
+            "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_grid",
+            "ug_get_weights", "ug_get_delays",
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
@@ -82,6 +83,11 @@ class RuntimeOpts(C.Structure):
                 ("use_graphs", C.c_int32)]
 
 
+class GroupItem(C.Structure):
+    _fields_ = [("net", C.c_int32), ("kind", C.c_int32), ("first_trial", C.c_uint32), ("n_trials", C.c_int32),
+                ("training", C.c_int32), ("status", C.c_int32)]
+
+
 _lib = None
 
 
@@ -105,6 +111,8 @@ def load_library(path: str = LIB_PATH):
     L.ug_run_test_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32]
     L.ug_get_trial_stats.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p]
     L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
+    L.ug_run_group.argtypes = [vp, C.POINTER(GroupItem), C.c_int32]
+    L.ug_set_group_grid.argtypes = [vp, C.c_int32, C.c_int32]
     L.ug_get_weights.argtypes = [vp, C.c_int32, _f64p]
     L.ug_get_delays.argtypes = [vp, C.c_int32, _f64p]
     L.ug_get_synapse_list.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p, C.POINTER(C.c_int64)]
@@ -282,6 +290,22 @@ class Engine:
         ms, n = C.c_double(0), C.c_int64(0)
         _check(self.L.ug_get_kernel_timing(self.ctx, kernel.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def run_group(self, items):
+        """Runs several resident networks together (ug_run_group).  items: sequence of
+        (network, kind, first_trial, n_trials, training) with kind "test" or "growth".
+        Returns the per-item status names; raises UGError on the first failure."""
+        arr = (GroupItem * len(items))()
+        for k, (rn, kind, first, n, training) in enumerate(items):
+            arr[k] = GroupItem(rn.id, 1 if kind == "growth" else 0, first, n, 1 if training else 0, 0)
+            rn.batch = n if kind == "test" else 1
+        st = self.L.ug_run_group(self.ctx, arr, len(items))
+        statuses = [UG_STATUS.get(arr[k].status, str(arr[k].status)) for k in range(len(items))]
+        _check(st)
+        return statuses
+
+    def set_group_grid(self, ra_blocks_per_sm: int = 0, i_blocks_per_sm: int = 0):
+        _check(self.L.ug_set_group_grid(self.ctx, ra_blocks_per_sm, i_blocks_per_sm))
 
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
