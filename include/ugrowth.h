@@ -150,6 +150,45 @@ ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items);
 /* Caps the blocks per SM of the group launches of the two integrators (0: the occupancy
  * limit).  The autotuner's knob. */
 ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm);
+/* Serving loop -- no counterpart in the reference.  A scheduler thread of the context
+ * runs group rounds (see ug_run_group) over the requests on the GPU and, between
+ * rounds, admits queued requests in arrival order while their device footprint fits
+ * the budget and a member slot is free, so requests that arrive while others run join
+ * the same launches.  A request's network is loaded at admission and stays loaded after
+ * completion under info.net_id: read the results with the getters, then free it with
+ * ug_free_network, which returns its bytes to the budget.  While the server runs, the
+ * context's other calls wait for the round in progress.  Start and stop the server
+ * from one thread. */
+enum { UG_REQ_QUEUED = 0, UG_REQ_RUNNING = 1, UG_REQ_DONE = 2, UG_REQ_FAILED = 3 };
+typedef struct {
+    int64_t hbm_budget_bytes;   /* device memory the served networks may hold (<= 0: 90% of the free memory) */
+    int32_t max_members;        /* most requests on the GPU at once (<= 0: 64) */
+} ug_server_opts;
+typedef struct {
+    const ug_network_desc* network;   /* copied before ug_submit returns */
+    int32_t kind;                     /* 0: test trials, 1: growth trials */
+    uint32_t first_trial;
+    int32_t n_trials;                 /* test: one batch; growth: consecutive trials */
+    int32_t training;                 /* growth: the training neurons get their kick */
+} ug_request;
+typedef struct {
+    int32_t state;                      /* UG_REQ_* */
+    int32_t status;                     /* ug_status of a finished request */
+    int32_t net_id;                     /* the request's network once admitted, else -1 */
+    int32_t trials_done;
+    double t_submit, t_admit, t_done;   /* seconds on a monotonic clock; -1 when not reached */
+    int64_t footprint_bytes;            /* device memory charged to the request */
+    char error[256];                    /* message of a failed request */
+} ug_request_info;
+ug_status ug_server_start(ug_ctx* ctx, const ug_server_opts* opts);
+/* UG_ENOMEM when the request can never fit the budget. */
+ug_status ug_submit(ug_ctx* ctx, const ug_request* request, uint64_t* request_id);
+/* State of a request (also after ug_server_stop); waits up to wait_seconds for it to
+ * finish (0: do not wait). */
+ug_status ug_poll(ug_ctx* ctx, uint64_t request_id, double wait_seconds, ug_request_info* info);
+/* Runs every submitted request to completion, then stops the scheduler thread. */
+ug_status ug_server_stop(ug_ctx* ctx);
+
 /* Dense n_ra x n_ra RA->RA weights (weights_RA_RA). */
 ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out);
 /* Dense n_ra x n_ra axonal delays (axonal_delays_RA_RA). */

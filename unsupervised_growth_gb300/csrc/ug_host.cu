@@ -15,8 +15,13 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <deque>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <memory>
 #include <string>
 #include <vector>
@@ -129,7 +134,13 @@ struct NetHost {
     std::vector<double> ra2i_len, i2ra_len;
     std::vector<int> mature, remodeled, tar;     // tar: trials after replacement
     std::vector<double> scale, frl;              // maturation scale, firing_rate_long
-    std::vector<int> hist;                       // [n_ra][window] newest first
+    // activity history per neuron: a ring of `window` spike counts, the k-th
+    // newest at (hist_head + k) % window, with running sums of the whole ring and
+    // of the trials with spikes among the newest 1000
+    std::vector<int> hist;                       // [n_ra][window]
+    int hist_head = 0;
+    std::vector<long long> hist_sum;
+    std::vector<int> hist_active;
     std::vector<double> ra_xyz, i_xyz;
 };
 
@@ -191,6 +202,8 @@ template <class R>
 class NetImpl : public NetBase {
 public:
     ug_status init(const ug_network_desc* d, int spike_cap_per_neuron, cudaStream_t st);
+    ug_status init_host(const ug_network_desc* d, int spike_cap_per_neuron);
+    ug_status init_device(cudaStream_t st);
     ug_status run_test_trials(uint32_t first_trial, int n_trials, const ug::LaunchCtx& lc, bool graphs,
                               int64_t* launches) override;
     ug_status stats(int which, int32_t* count, int32_t* first, cudaStream_t st) override;
@@ -216,6 +229,10 @@ public:
     ug_status finish_growth(uint32_t trial, int bad, cudaStream_t st);
     ug_status finish_test(cudaStream_t st) { return check_error(st); }
     size_t growth_row_count() const { return (size_t)h.n_ra; }
+    // Device bytes this network holds now, and the bytes it will hold once
+    // loaded and run as `kind` (0 test, 1 growth) with B instances.
+    size_t device_bytes() const;
+    size_t footprint(int kind, int B) const;
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -262,10 +279,20 @@ private:
         gNewpostCnt_, gSomaBits_, gBad_, gRep_, gStamp_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
+    std::vector<int> syncidx_;
+    std::vector<double> ra_decay_, i_decay_;
 };
 
 template <class R>
 ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, cudaStream_t st)
+{
+    UG_TRY(init_host(d, spike_cap_per_neuron));
+    return init_device(st);
+}
+
+// Host copy of the description, time tables and step constants; no device work.
+template <class R>
+ug_status NetImpl<R>::init_host(const ug_network_desc* d, int spike_cap_per_neuron)
 {
     NetHost& H = h;
     H.n_ra = d->n_ra;
@@ -319,9 +346,11 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
     }
 
     // time tables
-    std::vector<int> syncidx;
-    build_schedule(H.num_steps, T, sync_steps, syncidx);
-    std::vector<double> ra_decay((size_t)2 * H.num_steps, 1.0), i_decay((size_t)24 * H.num_steps, 1.0);
+    build_schedule(H.num_steps, T, sync_steps, syncidx_);
+    std::vector<double>& ra_decay = ra_decay_;
+    std::vector<double>& i_decay = i_decay_;
+    ra_decay.assign((size_t)2 * H.num_steps, 1.0);
+    i_decay.assign((size_t)24 * H.num_steps, 1.0);
     const double cnum[12] = {UG_DP_CNUM}, cden[12] = {UG_DP_CDEN};
     for (int s = 1; s < H.num_steps; ++s) {
         const double tm = T[s - 1];
@@ -370,6 +399,15 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
     H.frl.assign(NRA, 0.0);
     H.hist.assign((size_t)NRA * (win > 0 ? win : 0), 0);
     if (d->activity_history && win > 0) H.hist.assign(d->activity_history, d->activity_history + (size_t)NRA * win);
+    H.hist_head = 0;
+    H.hist_sum.assign(NRA, 0);
+    H.hist_active.assign(NRA, 0);
+    for (int i = 0; i < NRA && win > 0; ++i)
+        for (int k = 0; k < win; ++k) {
+            const int c = H.hist[(size_t)i * win + k];
+            H.hist_sum[i] += c;
+            if (k < 1000 && c > 0) H.hist_active[i] += 1;
+        }
     H.ra_xyz.assign((size_t)3 * NRA, 0.0);
     if (d->ra_xyz) H.ra_xyz.assign(d->ra_xyz, d->ra_xyz + (size_t)3 * NRA);
     H.i_xyz.assign((size_t)3 * NI, 0.0);
@@ -386,11 +424,25 @@ ug_status NetImpl<R>::init(const ug_network_desc* d, int spike_cap_per_neuron, c
                                             std::fabs(H.conn.delay_constant));
     if (!(max_delay >= 0.0) || max_delay > 1000.0) return fail(UG_EINVAL, "axonal delays must lie in [0, 1000] ms");
     ring = (int)std::floor(max_delay / 0.24) + 4;
+    return UG_OK;
+}
 
+// Device copy of the network (everything but the per-batch and growth buffers,
+// which are allocated on first use).
+template <class R>
+ug_status NetImpl<R>::init_device(cudaStream_t st)
+{
+    NetHost& H = h;
+    const int NRA = H.n_ra, NI = H.n_i;
     UG_TRY(dT_.upload(T, st));
-    UG_TRY(dSyncidx_.upload(syncidx, st));
-    UG_TRY(dRaDecay_.upload(ra_decay, st));
-    UG_TRY(dIDecay_.upload(i_decay, st));
+    UG_TRY(dSyncidx_.upload(syncidx_, st));
+    if (sizeof(R) == 8) {   // per-step decay tables: the double build only
+        UG_TRY(dRaDecay_.upload(ra_decay_, st));
+        UG_TRY(dIDecay_.upload(i_decay_, st));
+    } else {
+        UG_TRY(dRaDecay_.alloc(16));
+        UG_TRY(dIDecay_.alloc(16));
+    }
     std::vector<R> er(H.rest.begin(), H.rest.end()), gc(H.gca.begin(), H.gca.end());
     UG_TRY(dErest_.upload(er, st));
     UG_TRY(dGCa_.upload(gc, st));
@@ -546,6 +598,51 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
     UG_CUDA(cudaGraphLaunch(graph_exec_, st));
     if (launches) *launches += 2 * ((int64_t)sync_steps.size() + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
     return UG_OK;
+}
+
+template <class R>
+size_t NetImpl<R>::device_bytes() const
+{
+    size_t t = 0;
+    for (const DevMem* m : {&dT_, &dSyncidx_, &dRaDecay_, &dIDecay_, &dErest_, &dGCa_, &dSpread_, &dTraining_})
+        t += m->bytes();
+    for (const CsrDev* c : {&ra2i_, &i2ra_, &rara_}) t += c->off.bytes() + c->tgt.bytes() + c->wq.bytes() + c->d.bytes();
+    for (int k = 0; k < 10; ++k) t += ra_[k].bytes();
+    for (int k = 0; k < 7; ++k) t += iv_[k].bytes();
+    for (const DevMem* m : {&ra_flags_, &kick_step_, &ra_nsoma_, &ra_ndend_, &ra_first_soma_, &ra_first_dend_,
+                            &i_noise_, &i_noise_step_, &i_events_, &i_ev_idx_, &i_word_, &i_flag_, &i_nspk_, &i_first_,
+                            &ring_ra_exc_, &ring_ra_inh_, &ring_i_exc_, &spk_buf_, &spk_count_, &error_, &trial_,
+                            &mean_inj_})
+        t += m->bytes();
+    for (const DevMem* m : {&gW_, &gD_, &gPerm_, &gActive_, &gSuper_, &gActList_, &gActCnt_, &gSupList_, &gSupCnt_,
+                            &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gStStep_, &gStCur_, &gStLen_,
+                            &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_,
+                            &gStamp_})
+        t += m->bytes();
+    return t;
+}
+
+template <class R>
+size_t NetImpl<R>::footprint(int kind, int B) const
+{
+    const size_t S = (size_t)h.num_steps, nra = (size_t)h.n_ra, ni = (size_t)h.n_i, r = sizeof(R);
+    size_t act = 0;
+    for (const auto& a : h.active) act += a.size();
+    const size_t e_ri = h.ra2i_tgt.size(), e_ir = h.i2ra_tgt.size();
+    size_t t = 12 * S + (r == 8 ? 208 * S : 32) + nra * (2 * r + 9) + 16;
+    t += 4 * (nra + 1) + 20 * e_ri + 4 * (ni + 1) + 20 * e_ir + 4 * (nra + 1) + 20 * act;
+    if (kind == 1) B = 1;
+    const size_t bra = (size_t)B * nra, bi = (size_t)B * ni;
+    const size_t ev_cap = r == 4 ? (size_t)(h.num_steps * 0.02 * 0.25 * 2.0) + 64 : 1;
+    const size_t cap = (size_t)spike_cap_per_neuron_ * (2 * nra + ni);
+    t += bra * (10 * r + 24) + bi * (7 * r + 16 + 8 + 16 * ev_cap + 8 + 16);
+    t += (size_t)ring * 8 * (2 * bra + bi) + (size_t)B * (cap * 8 + 16);
+    if (kind == 1) {
+        const size_t nn = nra * nra;
+        t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 3 * 4 * ug::kMaxStreams +
+                              4 * ug::kMaxStreams * ug::kMaxNss + 8 + 64 + 4 + 4 + 4) + 8;
+    }
+    return t;
 }
 
 template <class R>
@@ -866,20 +963,23 @@ ug_status NetImpl<R>::after_growth_trial(uint32_t trial, cudaStream_t st)
     UG_CUDA(cudaStreamSynchronize(st));
     for (int i = 0; i < n; ++i) h.tar[i] += 1;
     std::vector<int> rep;
+    // push_front into the full circular buffer: the new count takes the slot of
+    // the oldest, and the 1000th newest leaves the robustness window (the sums
+    // are integers, so the rates equal the reference's full re-summation)
+    const int head = (h.hist_head + W - 1) % W;
+    const int leave = (h.hist_head + 999) % W;
     for (int i = 0; i < n; ++i) {
         int* hi = h.hist.data() + (size_t)i * W;
-        std::memmove(hi + 1, hi, (size_t)(W - 1) * sizeof(int));   // push_front into the full circular buffer
-        hi[0] = count[i];
-        double sum = 0.0;
-        for (int k = 0; k < W; ++k) sum += hi[k];
-        h.frl[i] = sum / (double)W;
-        double robust = 0.0;
-        for (int k = 0; k < 1000; ++k)
-            if (hi[k] > 0) robust += 1;
-        robust = robust / 1000.0;
+        const int oldest = hi[head], leaving = hi[leave];
+        hi[head] = count[i];
+        h.hist_sum[i] += count[i] - oldest;
+        h.hist_active[i] += (count[i] > 0 ? 1 : 0) - (leaving > 0 ? 1 : 0);
+        h.frl[i] = (double)h.hist_sum[i] / (double)W;
+        const double robust = (double)h.hist_active[i] / 1000.0;
         if (robust >= 0.5 && h.scale[i] != 1000.0) h.scale[i] = 1000.0;   // MATURATION_SCALE_DRIVEN
         if (robust < h.mat.DEATH_RATE_THRESHOLD && h.tar[i] > 1000) rep.push_back(i);
     }
+    h.hist_head = head;
     for (int i = 0; i < n; ++i) {
         if (h.mature[i] == 1) continue;
         h.rest[i] = h.rest[i] + (h.rest[i] - h.mat.E_REST_MATURE) * (std::exp(-1.0 / h.scale[i]) - 1);
@@ -1018,6 +1118,8 @@ ug_status NetImpl<R>::replace_neurons(const std::vector<int>& rep, uint32_t tria
         h.tar[r] = 0;
         std::fill(h.hist.begin() + (size_t)r * h.mat.RATE_WINDOW_LONG,
                   h.hist.begin() + (size_t)(r + 1) * h.mat.RATE_WINDOW_LONG, 0);
+        h.hist_sum[r] = 0;
+        h.hist_active[r] = 0;
     }
     // device copies of the delays, their target order and the RA<->I lists
     UG_CUDA(cudaMemcpyAsync(gD_.as<double>(), h.D.data(), h.D.size() * sizeof(double), cudaMemcpyHostToDevice, st));
@@ -1293,6 +1395,8 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
 
 }  // namespace
 
+class Server;
+
 struct ug_ctx {
     int precision = 32;
     int device = 0;
@@ -1318,6 +1422,9 @@ struct ug_ctx {
     std::map<int, std::unique_ptr<NetBase>> nets;
     std::unique_ptr<GroupBase> group;          // GroupExec<float> or GroupExec<double>
     int group_ra_bps = 0, group_i_bps = 0;     // integrator blocks per SM of group launches (0: occupancy)
+    std::recursive_mutex mu;                   // one caller at a time: API calls and the server's rounds
+    std::unique_ptr<Server> server;
+    ~ug_ctx();
 };
 
 namespace {
@@ -1332,6 +1439,257 @@ ug_status get_net(ug_ctx* c, int id, NetBase** out)
 }
 
 }  // namespace
+
+
+// ---------------------------------------------------------------------------
+// Serving loop (ug_server_start / ug_submit / ug_poll / ug_server_stop).
+//
+// A scheduler thread runs group rounds (one trial of every running request,
+// a test request's whole batch in its first round) and, between rounds,
+// admits queued requests in arrival order while their device footprint fits
+// the budget and a member slot is free: requests that arrive while others are
+// on the GPU join the next round, and their trials run in the same launches
+// as everyone else's.  A request's network stays loaded after completion
+// under the id ug_poll reports; ug_free_network returns its bytes to the budget.
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServerReq {
+    uint64_t id = 0;
+    int kind = 0;
+    uint32_t first_trial = 0;
+    int n_trials = 0;
+    int training = 0;
+    std::unique_ptr<NetBase> net;   // host copy until admission
+    int net_id = -1;
+    int state = UG_REQ_QUEUED;
+    ug_status status = UG_OK;
+    std::string error;
+    int trials_done = 0;
+    double t_submit = 0.0, t_admit = -1.0, t_done = -1.0;
+    int64_t footprint = 0;
+};
+
+}  // namespace
+
+class Server {
+public:
+    Server(ug_ctx* c, int64_t budget, int max_members) : ctx_(c), budget_(budget), max_members_(max_members)
+    {
+        th_ = std::thread([this] { loop(); });
+    }
+    ~Server() { stop(); }
+    ug_status submit(const ug_request* r, uint64_t* id);
+    ug_status poll(uint64_t id, double wait_s, ug_request_info* out);
+    void stop()
+    {
+        {
+            std::lock_guard<std::mutex> lk(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        if (th_.joinable()) th_.join();
+    }
+    bool stopped()
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        return stop_;
+    }
+    // A network of a request that is still running.
+    bool busy(int net_id)
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        for (const ServerReq* r : running_)
+            if (r->net_id == net_id) return true;
+        return false;
+    }
+    void release(int net_id)
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        auto it = owned_.find(net_id);
+        if (it == owned_.end()) return;
+        used_ -= it->second;
+        owned_.erase(it);
+        cv_.notify_all();
+    }
+
+private:
+    void loop();
+    template <class R>
+    void round();
+    void finish(ServerReq* r, ug_status s, const std::string& msg, double t)
+    {
+        r->status = s;
+        r->state = s == UG_OK ? UG_REQ_DONE : UG_REQ_FAILED;
+        r->error = msg;
+        r->t_done = t;
+    }
+
+    ug_ctx* ctx_;
+    std::thread th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_cv_;
+    bool stop_ = false;
+    uint64_t next_ = 1;
+    std::deque<ServerReq*> queue_;
+    std::vector<ServerReq*> running_;
+    std::map<uint64_t, std::unique_ptr<ServerReq>> reqs_;
+    std::map<int, int64_t> owned_;   // loaded network id -> bytes charged
+    int64_t budget_, used_ = 0;
+    int max_members_;
+};
+
+ug_status Server::submit(const ug_request* q, uint64_t* id)
+{
+    if (!q || !q->network || !id) return fail(UG_EINVAL, "null request");
+    if (q->kind != 0 && q->kind != 1) return fail(UG_EINVAL, "request kind must be 0 (test) or 1 (growth)");
+    if (q->n_trials <= 0 || (q->kind == 0 && q->n_trials > 65535)) return fail(UG_EINVAL, "bad n_trials");
+    std::unique_ptr<ServerReq> r(new ServerReq());
+    r->kind = q->kind;
+    r->first_trial = q->first_trial;
+    r->n_trials = q->n_trials;
+    r->training = q->training;
+    if (ctx_->precision == 64) {
+        auto* p = new NetImpl<double>();
+        r->net.reset(p);
+        UG_TRY(p->init_host(q->network, ctx_->spike_cap));
+        r->footprint = (int64_t)p->footprint(q->kind, q->n_trials);
+    } else {
+        auto* p = new NetImpl<float>();
+        r->net.reset(p);
+        UG_TRY(p->init_host(q->network, ctx_->spike_cap));
+        r->footprint = (int64_t)p->footprint(q->kind, q->n_trials);
+    }
+    if (r->footprint > budget_) return fail(UG_ENOMEM, "request needs more device memory than the server's budget");
+    r->t_submit = now_s();
+    {
+        std::lock_guard<std::mutex> lk(m_);
+        if (stop_) return fail(UG_EINVAL, "the server is stopping");
+        r->id = next_++;
+        *id = r->id;
+        queue_.push_back(r.get());
+        reqs_[r->id] = std::move(r);
+    }
+    cv_.notify_all();
+    return UG_OK;
+}
+
+ug_status Server::poll(uint64_t id, double wait_s, ug_request_info* out)
+{
+    std::unique_lock<std::mutex> lk(m_);
+    auto it = reqs_.find(id);
+    if (it == reqs_.end()) return fail(UG_EINVAL, "unknown request id");
+    ServerReq* r = it->second.get();
+    if (wait_s > 0.0)
+        done_cv_.wait_for(lk, std::chrono::duration<double>(wait_s), [r] { return r->state >= UG_REQ_DONE; });
+    if (out) {
+        out->state = r->state;
+        out->status = r->status;
+        out->net_id = r->net_id;
+        out->trials_done = r->trials_done;
+        out->t_submit = r->t_submit;
+        out->t_admit = r->t_admit;
+        out->t_done = r->t_done;
+        out->footprint_bytes = r->footprint;
+        std::snprintf(out->error, sizeof(out->error), "%s", r->error.c_str());
+    }
+    return UG_OK;
+}
+
+void Server::loop()
+{
+    cudaSetDevice(ctx_->device);
+    while (true) {
+        std::vector<ServerReq*> admit;
+        {
+            std::unique_lock<std::mutex> lk(m_);
+            cv_.wait(lk, [this] { return stop_ || !queue_.empty() || !running_.empty(); });
+            if (queue_.empty() && running_.empty()) {
+                if (stop_) return;
+                continue;
+            }
+            // arrival order: a request that does not fit yet holds back the ones behind it
+            while (!queue_.empty() && (int)(running_.size() + admit.size()) < max_members_) {
+                ServerReq* r = queue_.front();
+                if (used_ + r->footprint > budget_) break;
+                used_ += r->footprint;
+                admit.push_back(r);
+                queue_.pop_front();
+            }
+            if (admit.empty() && running_.empty()) {
+                // nothing fits until a finished request's network is freed
+                cv_.wait_for(lk, std::chrono::milliseconds(50));
+                continue;
+            }
+        }
+        std::lock_guard<std::recursive_mutex> g(ctx_->mu);
+        for (ServerReq* r : admit) {
+            ug_status s = UG_OK;
+            if (ctx_->precision == 64) s = static_cast<NetImpl<double>*>(r->net.get())->init_device(ctx_->stream);
+            else s = static_cast<NetImpl<float>*>(r->net.get())->init_device(ctx_->stream);
+            std::lock_guard<std::mutex> lk(m_);
+            if (s != UG_OK) {
+                finish(r, s, g_err, now_s());
+                used_ -= r->footprint;
+                r->net.reset();
+                done_cv_.notify_all();
+                continue;
+            }
+            const int nid = ctx_->next_id++;
+            ctx_->nets[nid] = std::move(r->net);
+            owned_[nid] = r->footprint;
+            r->net_id = nid;
+            r->t_admit = now_s();
+            r->state = UG_REQ_RUNNING;
+            running_.push_back(r);
+        }
+        if (running_.empty()) continue;
+        if (ctx_->precision == 64) round<double>();
+        else round<float>();
+    }
+}
+
+template <class R>
+void Server::round()
+{
+    if (!ctx_->group) ctx_->group.reset(new GroupExec<R>());
+    GroupExec<R>* ge = static_cast<GroupExec<R>*>(ctx_->group.get());
+    std::vector<RoundItem<R>> items;
+    for (ServerReq* r : running_) {
+        auto* n = static_cast<NetImpl<R>*>(ctx_->nets[r->net_id].get());
+        if (r->kind == 0) items.push_back({n, 0, r->first_trial, r->n_trials, 1, UG_OK});
+        else items.push_back({n, 1, r->first_trial + (uint32_t)r->trials_done, 1, r->training, UG_OK});
+    }
+    const ug_status s = ge->run_round(items, ctx_->launch_ctx(), ctx_->graphs, ctx_->group_ra_bps, ctx_->group_i_bps,
+                                      &ctx_->launches);
+    const std::string msg = g_err;
+    const double t = now_s();
+    bool attributed = false;
+    for (const RoundItem<R>& it : items) attributed |= it.status != UG_OK;
+    std::lock_guard<std::mutex> lk(m_);
+    std::vector<ServerReq*> still;
+    for (size_t j = 0; j < running_.size(); ++j) {
+        ServerReq* r = running_[j];
+        const ug_status sj = attributed ? items[j].status : s;
+        if (sj != UG_OK) {
+            finish(r, sj, msg, t);
+            continue;
+        }
+        r->trials_done += r->kind == 0 ? r->n_trials : 1;
+        if (r->trials_done >= r->n_trials) finish(r, UG_OK, "", t);
+        else still.push_back(r);
+    }
+    running_.swap(still);
+    done_cv_.notify_all();
+}
+
+
+ug_ctx::~ug_ctx() = default;
 
 namespace {
 template <class R>
@@ -1417,6 +1775,8 @@ ug_status ug_create(ug_ctx** out, const ug_runtime_opts* opts)
 void ug_destroy(ug_ctx* ctx)
 {
     if (!ctx) return;
+    if (ctx->server) ctx->server->stop();   // outside the context lock: the last rounds need it
+    ctx->server.reset();
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     cudaStreamSynchronize(ctx->side);
@@ -1433,12 +1793,16 @@ void ug_destroy(ug_ctx* ctx)
 ug_status ug_set_stream(ug_ctx* ctx, void* stream)
 {
     if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    if (!ctx) return fail(UG_EINVAL, "null context");
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own;
     return UG_OK;
 }
 
 ug_status ug_synchronize(ug_ctx* ctx)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     if (!ctx) return fail(UG_EINVAL, "null context");
     UG_CUDA(cudaSetDevice(ctx->device));
     UG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1447,6 +1811,8 @@ ug_status ug_synchronize(ug_ctx* ctx)
 
 ug_status ug_load_network(ug_ctx* ctx, const ug_network_desc* desc, int32_t* net_id)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     if (!ctx || !desc || !net_id) return fail(UG_EINVAL, "null argument");
     UG_CUDA(cudaSetDevice(ctx->device));
     std::unique_ptr<NetBase> net;
@@ -1469,15 +1835,21 @@ ug_status ug_load_network(ug_ctx* ctx, const ug_network_desc* desc, int32_t* net
 
 ug_status ug_free_network(ug_ctx* ctx, int32_t net_id)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->server && ctx->server->busy(net_id)) return fail(UG_EINVAL, "the network's request is still running");
     ctx->nets.erase(net_id);
+    if (ctx->server) ctx->server->release(net_id);
     return UG_OK;
 }
 
 ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaSetDevice(ctx->device));
@@ -1486,6 +1858,8 @@ ug_status ug_run_test_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, 
 
 ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial, int32_t n_trials, int32_t training)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     UG_CUDA(cudaSetDevice(ctx->device));
@@ -1495,6 +1869,8 @@ ug_status ug_run_growth_trials(ug_ctx* ctx, int32_t net_id, uint32_t first_trial
 
 ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     if (!ctx) return fail(UG_EINVAL, "null context");
     if (n_items < 0 || (n_items > 0 && !items)) return fail(UG_EINVAL, "bad group item array");
     if (n_items == 0) return UG_OK;
@@ -1506,14 +1882,57 @@ ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items)
 ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm)
 {
     if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    if (!ctx) return fail(UG_EINVAL, "null context");
     if (ra_blocks_per_sm < 0 || i_blocks_per_sm < 0) return fail(UG_EINVAL, "blocks per SM must be >= 0");
     ctx->group_ra_bps = ra_blocks_per_sm;
     ctx->group_i_bps = i_blocks_per_sm;
     return UG_OK;
 }
 
+ug_status ug_server_start(ug_ctx* ctx, const ug_server_opts* opts)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    if (ctx->server && !ctx->server->stopped()) return fail(UG_EINVAL, "the server is already running");
+    UG_CUDA(cudaSetDevice(ctx->device));
+    int64_t budget = opts ? opts->hbm_budget_bytes : 0;
+    if (budget <= 0) {
+        size_t fr = 0, tot = 0;
+        UG_CUDA(cudaMemGetInfo(&fr, &tot));
+        budget = (int64_t)(0.9 * (double)fr);
+    }
+    const int mm = opts && opts->max_members > 0 ? opts->max_members : 64;
+    ctx->server.reset(new Server(ctx, budget, mm));
+    return UG_OK;
+}
+
+ug_status ug_submit(ug_ctx* ctx, const ug_request* request, uint64_t* request_id)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    if (!ctx->server) return fail(UG_EINVAL, "the server is not running (ug_server_start)");
+    return ctx->server->submit(request, request_id);
+}
+
+ug_status ug_poll(ug_ctx* ctx, uint64_t request_id, double wait_seconds, ug_request_info* info)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    if (!ctx->server) return fail(UG_EINVAL, "the server is not running (ug_server_start)");
+    return ctx->server->poll(request_id, wait_seconds, info);
+}
+
+ug_status ug_server_stop(ug_ctx* ctx)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    if (!ctx->server) return UG_OK;
+    ctx->server->stop();   // without the context lock: the remaining rounds take it
+    return UG_OK;
+}
+
 ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (!out) return fail(UG_EINVAL, "null output");
@@ -1522,6 +1941,8 @@ ug_status ug_get_weights(ug_ctx* ctx, int32_t net_id, double* out)
 
 ug_status ug_get_delays(ug_ctx* ctx, int32_t net_id, double* out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (!out) return fail(UG_EINVAL, "null output");
@@ -1532,6 +1953,8 @@ ug_status ug_get_delays(ug_ctx* ctx, int32_t net_id, double* out)
 ug_status ug_get_synapse_list(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
                               int64_t* total)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (which != 0 && which != 1) return fail(UG_EINVAL, "which must be 0 or 1");
@@ -1542,6 +1965,8 @@ ug_status ug_get_neuron_props(ug_ctx* ctx, int32_t net_id, double* rest_potentia
                               double* maturation_scale, int32_t* remodeled, int32_t* trials_after_replacement,
                               double* firing_rate_long)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     return n->neuron_props(rest_potential, gca, mature, maturation_scale, remodeled, trials_after_replacement,
@@ -1550,6 +1975,8 @@ ug_status ug_get_neuron_props(ug_ctx* ctx, int32_t net_id, double* rest_potentia
 
 ug_status ug_get_replaced(ug_ctx* ctx, int32_t net_id, int32_t* out, int64_t capacity, int64_t* n_out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (n_out) *n_out = (int64_t)n->replaced.size();
@@ -1560,6 +1987,8 @@ ug_status ug_get_replaced(ug_ctx* ctx, int32_t net_id, int32_t* out, int64_t cap
 ug_status ug_get_connections(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* offsets, int32_t* targets,
                              double* weights, double* delays, int64_t* total)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (which != 0 && which != 1) return fail(UG_EINVAL, "which must be 0 or 1");
@@ -1578,6 +2007,8 @@ ug_status ug_get_connections(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t
 
 ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double* i_xyz)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (ra_xyz) std::copy(n->h.ra_xyz.begin(), n->h.ra_xyz.end(), ra_xyz);
@@ -1587,6 +2018,8 @@ ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double
 
 ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t* count, int32_t* first_step)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (which < 0 || which > 2) return fail(UG_EINVAL, "which must be 0, 1 or 2");
@@ -1596,6 +2029,8 @@ ug_status ug_get_trial_stats(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t
 ug_status ug_get_spikes(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t which, int32_t* neuron, int32_t* step,
                         int64_t capacity, int64_t* n_out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (which < 0 || which > 2) return fail(UG_EINVAL, "which must be 0, 1 or 2");
@@ -1604,6 +2039,8 @@ ug_status ug_get_spikes(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t w
 
 ug_status ug_get_neuron_state(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t which, double* out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if ((which != 0 && which != 1) || !out) return fail(UG_EINVAL, "bad argument");
@@ -1612,6 +2049,8 @@ ug_status ug_get_neuron_state(ug_ctx* ctx, int32_t net_id, int32_t instance, int
 
 ug_status ug_step_time(ug_ctx* ctx, int32_t net_id, int32_t step, double* t)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (step < 0 || step >= (int)n->T.size() || !t) return fail(UG_EINVAL, "step out of range");
@@ -1622,6 +2061,8 @@ ug_status ug_step_time(ug_ctx* ctx, int32_t net_id, int32_t step, double* t)
 ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled)
 {
     if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    if (!ctx) return fail(UG_EINVAL, "null context");
     UG_CUDA(cudaStreamSynchronize(ctx->stream));
     UG_CUDA(ctx->timer.collect());
     ctx->timer.clear(false);
@@ -1631,6 +2072,8 @@ ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled)
 
 ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     if (!ctx || !kernel || !total_ms || !launches) return fail(UG_EINVAL, "null argument");
     UG_CUDA(ctx->timer.collect());
     long long n = 0;
@@ -1641,6 +2084,8 @@ ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms
 
 ug_status ug_launch_count(ug_ctx* ctx, int64_t* out)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     if (!ctx || !out) return fail(UG_EINVAL, "null argument");
     *out = ctx->launches;
     return UG_OK;
@@ -1709,6 +2154,8 @@ extern "C" ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint
                                                int32_t* soma_first, int32_t* dend_count, int32_t* dend_first,
                                                int32_t* inter_count, int32_t* inter_first)
 {
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     NetBase* net;
     UG_TRY(get_net(ctx, net_id, &net));
     if (!soma_count || !soma_first || !dend_count || !dend_first || !inter_count || !inter_first)

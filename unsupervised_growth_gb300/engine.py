@@ -24,7 +24,7 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
             "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_grid",
-            "ug_get_weights", "ug_get_delays",
+            "ug_server_start", "ug_submit", "ug_poll", "ug_server_stop", "ug_get_weights", "ug_get_delays",
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
@@ -88,6 +88,23 @@ class GroupItem(C.Structure):
                 ("training", C.c_int32), ("status", C.c_int32)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_int64), ("max_members", C.c_int32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("network", C.c_void_p), ("kind", C.c_int32), ("first_trial", C.c_uint32), ("n_trials", C.c_int32),
+                ("training", C.c_int32)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("net_id", C.c_int32), ("trials_done", C.c_int32),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("footprint_bytes", C.c_int64), ("error", C.c_char * 256)]
+
+
+REQUEST_STATE = {0: "queued", 1: "running", 2: "done", 3: "failed"}
+
 _lib = None
 
 
@@ -113,6 +130,10 @@ def load_library(path: str = LIB_PATH):
     L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
     L.ug_run_group.argtypes = [vp, C.POINTER(GroupItem), C.c_int32]
     L.ug_set_group_grid.argtypes = [vp, C.c_int32, C.c_int32]
+    L.ug_server_start.argtypes = [vp, C.POINTER(ServerOpts)]
+    L.ug_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
+    L.ug_poll.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]
+    L.ug_server_stop.argtypes = [vp]
     L.ug_get_weights.argtypes = [vp, C.c_int32, _f64p]
     L.ug_get_delays.argtypes = [vp, C.c_int32, _f64p]
     L.ug_get_synapse_list.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p, C.POINTER(C.c_int64)]
@@ -306,6 +327,36 @@ class Engine:
 
     def set_group_grid(self, ra_blocks_per_sm: int = 0, i_blocks_per_sm: int = 0):
         _check(self.L.ug_set_group_grid(self.ctx, ra_blocks_per_sm, i_blocks_per_sm))
+
+    # ---- serving loop
+    def server_start(self, hbm_budget_bytes: int = 0, max_members: int = 0):
+        _check(self.L.ug_server_start(self.ctx, C.byref(ServerOpts(hbm_budget_bytes, max_members))))
+
+    def submit(self, net: Network, kind: str, first_trial: int, n_trials: int, training: bool = True) -> int:
+        """Queues a request on the server; the network is copied before this returns."""
+        d, keep = make_desc(net)
+        req = Request(C.cast(C.pointer(d), C.c_void_p), 1 if kind == "growth" else 0, first_trial, n_trials,
+                      1 if training else 0)
+        rid = C.c_uint64(0)
+        _check(self.L.ug_submit(self.ctx, C.byref(req), C.byref(rid)))
+        return rid.value
+
+    def poll(self, request_id: int, wait_seconds: float = 0.0) -> dict:
+        info = RequestInfo()
+        _check(self.L.ug_poll(self.ctx, request_id, wait_seconds, C.byref(info)))
+        return dict(state=REQUEST_STATE[info.state], status=UG_STATUS.get(info.status, str(info.status)),
+                    net_id=info.net_id, trials_done=info.trials_done, t_submit=info.t_submit,
+                    t_admit=info.t_admit, t_done=info.t_done, footprint_bytes=info.footprint_bytes,
+                    error=info.error.decode(errors="replace"))
+
+    def server_stop(self):
+        _check(self.L.ug_server_stop(self.ctx))
+
+    def adopt(self, net: Network, net_id: int, kind: str, n_trials: int) -> "ResidentNetwork":
+        """The resident network of a finished request (the getters read its results)."""
+        rn = ResidentNetwork(self, net, net_id)
+        rn.batch = n_trials if kind == "test" else 1
+        return rn
 
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
