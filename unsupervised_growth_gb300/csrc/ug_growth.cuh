@@ -285,59 +285,73 @@ struct RowShared {
     double td[2][kDueCap];     // gathered / ranked delivery times
     int tgt[2][kDueCap];
     int spk[2][kDueCap];       // spike step of the event's stream (streams are in spike order)
-    int newc[kMaxStreams];     // stream cursors after the gather
-    int rs[kMaxStreams + 1];   // start of each stream's run in the gather buffer
+    int rs[kMaxStreams + 1];   // start of each run (one per stream with due events) in the gather buffer
+    int rq[kMaxStreams];       // the run's stream (position in the row's stream ring)
+    int rtr[kMaxStreams];      // the run stopped at its quota with more due events behind
 };
 
-// Gathers every event of row r due by Tlim: each stream's due events are a
-// prefix of its remaining targets (delivery times rise along a stream).
-// Returns the event count, or -1 when they do not fit; cursors are committed
-// only on success.  nrun = streams that contributed events.
+// Gathers the events of row i due by Tlim, at most `quota` per stream: each
+// stream's due events are a prefix of its remaining targets (delivery times
+// rise along a stream), so a run is that prefix, cut at the quota.  Cursors
+// are not moved here.  Returns the event count; nrun runs, truncated = some
+// run stopped at its quota with more due events behind it.
 template <class R>
-__device__ __forceinline__ int g_gather(const GrowthDev& g, const NetDev<R>& n, double Tlim, int head, int num,
-                                        const int* stS, int* stC, const int* stL, const int* stT, const int* perm,
-                                        const double* Drow, RowShared& sh, int lane, int& nrun)
+__device__ __forceinline__ int g_gather(const NetDev<R>& n, double Tlim, int head, int num, const int* stS,
+                                        const int* stC, const int* stL, const int* stT, const int* perm,
+                                        const double* Drow, RowShared& sh, int lane, int quota, int& nrun,
+                                        bool& truncated)
 {
     int total = 0;
     nrun = 0;
+    truncated = false;
     for (int q = 0; q < num; ++q) {
         const int slot = (head + q) % kMaxStreams;
         const int L = stL[slot];
         const int len = L < 0 ? -L : L;
-        int c = stC[slot];
+        const int c = stC[slot];
         const int spk = stS[slot];
         const double Tsp = n.T[spk];
         const int start = total;
-        while (c < len) {
-            const int idx = c + lane;
+        int taken = 0;
+        while (c + taken < len && taken < quota) {
+            const int k = taken + lane;
+            const int idx = c + k;
             bool due = false;
             double td = 0.0;
             int t = 0;
-            if (idx < len) {
+            if (idx < len && k < quota) {
                 t = L < 0 ? stT[slot * kMaxNss + idx] : perm[idx];
                 td = Tsp + Drow[t];
                 due = Tlim >= td;
             }
             const int nd = __popc(__ballot_sync(0xffffffffu, due));
-            if (total + nd > kDueCap) return -1;
             if (due) {
                 sh.td[0][total + lane] = td;
                 sh.tgt[0][total + lane] = t;
                 sh.spk[0][total + lane] = spk;
             }
             total += nd;
-            c += nd;
+            taken += nd;
             if (nd < 32) break;
         }
-        if (lane == 0) sh.newc[q] = c;
-        if (total > start) {
-            if (lane == 0) sh.rs[nrun] = start;
+        bool trunc = false;
+        if (taken == quota && c + taken < len) {
+            const int idx = c + taken;
+            const int t = L < 0 ? stT[slot * kMaxNss + idx] : perm[idx];
+            trunc = Tlim >= Tsp + Drow[t];
+        }
+        if (taken > 0) {
+            if (lane == 0) {
+                sh.rs[nrun] = start;
+                sh.rq[nrun] = q;
+                sh.rtr[nrun] = trunc ? 1 : 0;
+            }
             ++nrun;
         }
+        truncated |= trunc;
     }
     if (lane == 0) sh.rs[nrun] = total;
     __syncwarp();
-    for (int q = lane; q < num; q += 32) stC[(head + q) % kMaxStreams] = sh.newc[q];
     return total;
 }
 
@@ -350,7 +364,7 @@ __device__ __forceinline__ bool ev_less(double ta, int ga, int sa, double tb, in
 // Ranks the gathered events into buffer 1 in queue order.  Runs are merged by
 // binary search; a run whose (time, target) order differs from its (delay,
 // target) order (delivery times that round equal) takes the quadratic rank.
-__device__ __forceinline__ void g_rank(RowShared& sh, int total, int nrun, int lane)
+__device__ __forceinline__ bool g_rank(RowShared& sh, int total, int nrun, int lane)
 {
     bool sorted = true;
     for (int e = lane; e + 1 < total; e += 32)
@@ -397,6 +411,7 @@ __device__ __forceinline__ void g_rank(RowShared& sh, int total, int nrun, int l
         }
     }
     __syncwarp();
+    return sorted;
 }
 
 // Processes the ranked events of row i, 32 at a time.  An event is delivered
@@ -515,24 +530,71 @@ __device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, con
         }
         const uint32_t later = (sa - s0 + 1) < 32 ? bits >> (sa - s0 + 1) : 0u;
         const int sb = later ? sa + __ffs(later) - 1 : s1;
-        int nrun = 0;
-        int total = num > 0 ? g_gather(g, n, sh_T[sb - s0], head, num, stS, stC, stL, stT, perm, Drow, sh, lane, nrun)
-                            : 0;
-        if (total > 0) {
-            g_rank(sh, total, nrun, lane);
-            g_process(g, n, bt, b, i, r, sa, sh_T + (sa - s0), total, sh, lane);
-        } else if (total < 0) {
-            for (int s = sa; s <= sb; ++s) {
-                total = g_gather(g, n, sh_T[s - s0], head, num, stS, stC, stL, stT, perm, Drow, sh, lane, nrun);
-                if (total > 0) {
-                    g_rank(sh, total, nrun, lane);
-                    g_process(g, n, bt, b, i, r, s, sh_T + (s - s0), total, sh, lane);
-                } else if (total < 0) {
-                    if (lane == 0)
-                        g_drain_seq(g, n, bt, b, i, s, sh_T[s - s0], head, num, stS, stC, stL, stT, perm, Drow);
+        // Chunks in queue order: gather up to `quota` due events per stream,
+        // rank them, and process those no later (in queue order) than the last
+        // gathered event of every stream cut at its quota -- no event left
+        // behind can precede them.  Then move each stream's cursor past its
+        // processed prefix and gather again.
+        const int quota = num > 0 ? kDueCap / num : kDueCap;
+        while (num > 0) {
+            int nrun = 0;
+            bool trunc = false;
+            const int total = g_gather(n, sh_T[sb - s0], head, num, stS, stC, stL, stT, perm, Drow, sh, lane, quota,
+                                       nrun, trunc);
+            if (total == 0) break;
+            const bool sorted = g_rank(sh, total, nrun, lane);
+            if (!sorted && trunc) {
+                // a stream whose (delay, target) order differs from its queue
+                // order and does not fit: deliver step by step, one event at a time
+                for (int s = sa; s <= sb; ++s) {
+                    if (lane == 0) g_drain_seq(g, n, bt, b, i, s, sh_T[s - s0], head, num, stS, stC, stL, stT, perm, Drow);
                     __syncwarp();
                 }
+                break;
             }
+            // the cut: smallest last key among the truncated runs
+            double ct = 0.0;
+            int cg = 0, cs = 0, P = total;
+            if (trunc) {
+                bool have = false;
+                for (int k = 0; k < nrun; ++k) {
+                    if (!sh.rtr[k]) continue;
+                    const int e = sh.rs[k + 1] - 1;
+                    const double te = sh.td[0][e];
+                    const int ge = sh.tgt[0][e], se = sh.spk[0][e];
+                    if (!have || ev_less(te, ge, se, ct, cg, cs)) {
+                        ct = te;
+                        cg = ge;
+                        cs = se;
+                        have = true;
+                    }
+                }
+                int lo = 0, hi = total;   // ranked events not after the cut
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (!ev_less(ct, cg, cs, sh.td[1][mid], sh.tgt[1][mid], sh.spk[1][mid])) lo = mid + 1;
+                    else hi = mid;
+                }
+                P = lo;
+            }
+            g_process(g, n, bt, b, i, r, sa, sh_T + (sa - s0), P, sh, lane);
+            // advance each stream past its processed prefix
+            if (lane < nrun) {
+                const int a0 = sh.rs[lane], a1 = sh.rs[lane + 1];
+                int adv = a1 - a0;
+                if (trunc) {
+                    int lo = a0, hi = a1;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (!ev_less(ct, cg, cs, sh.td[0][mid], sh.tgt[0][mid], sh.spk[0][mid])) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    adv = lo - a0;
+                }
+                stC[(head + sh.rq[lane]) % kMaxStreams] += adv;
+            }
+            __syncwarp();
+            if (!trunc) break;
         }
         // retire exhausted streams at the head of the ring
         while (num > 0) {
