@@ -357,6 +357,203 @@ def run_growth(args, local_rank):
     return result
 
 
+def _device_name(device):
+    import torch
+    return torch.cuda.get_device_name(device).replace(" ", "_")
+
+
+def _fp64_plain_seconds(nets, device, kind):
+    """Seconds per trial of the plain double-precision path (one trial, no batching,
+    no graph) for each network."""
+    from unsupervised_growth_gb300.engine import Engine
+    eng = Engine(precision=64, device=device, use_graphs=False)
+    out = []
+    for net in nets:
+        rn = eng.load_network(net)
+        t0 = time.perf_counter()
+        if kind == "growth":
+            rn.run_growth_trials(0, 1, True)
+        else:
+            rn.run_test_trials(0, 1)
+        eng.synchronize()
+        out.append(time.perf_counter() - t0)
+        rn.free()
+    eng.close()
+    return out
+
+
+def _interp_loglog(xs, ys, x):
+    import numpy as np
+    order = np.argsort(xs)
+    lx, ly = np.log(np.asarray(xs, float)[order]), np.log(np.asarray(ys, float)[order])
+    if len(lx) == 1:
+        return float(ys[0] * x / xs[0])
+    k = int(np.clip(np.searchsorted(lx, np.log(x)) - 1, 0, len(lx) - 2))
+    slope = (ly[k + 1] - ly[k]) / (lx[k + 1] - lx[k]) if lx[k + 1] > lx[k] else 1.0
+    return float(np.exp(ly[k] + slope * (np.log(x) - lx[k])))
+
+
+def run_uneven(args, local_rank):
+    """Batched growth of many networks of uneven size: one step = one group round,
+    i.e. one growth trial of every network, all stepped by the same launches."""
+    from unsupervised_growth_gb300 import autotune
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    from unsupervised_growth_gb300.workloads import uneven_networks
+    B.build()
+    nets = uneven_networks(args.members)
+    eng = Engine(precision=32, device=local_rank)
+    rns = [eng.load_network(n) for n in nets]
+    trial = [0]
+
+    def one_round():
+        eng.run_group([(rn, "growth", trial[0], 1, True) for rn in rns])
+        trial[0] += 1
+
+    one_round()   # first round: growth state set-up and graph capture
+    sig = autotune.signature(_device_name(local_rank), [(n.n_ra, "growth", 1) for n in nets])
+    tuned = autotune.tune(eng, one_round, sig=sig, max_rounds=max(args.warmup, 6))
+    while trial[0] < args.warmup:
+        one_round()
+    l0 = eng.launch_count()
+    with ClockSampler(local_rank) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            one_round()
+        wall = time.perf_counter() - t0
+    launches = eng.launch_count() - l0
+    eng.set_kernel_timing(True)
+    one_round()
+    names = ("k_trial_init", "k_noise_events", "k_growth_reset", "k_interval_ra", "k_interval_i", "k_growth_rows",
+             "k_growth_newpost", "k_growth_ltp", "k_growth_epilogue", "k_check_bad")
+    kt = {k: round(eng.kernel_timing(k)[0], 3) for k in names}
+    eng.set_kernel_timing(False)
+    neurons = sum(n.n_ra + n.n_i for n in nets)
+    res = {"metric": f"growth trials/s ({len(nets)} growing networks of uneven size, one group)",
+           "value": len(nets) * args.steps / wall, "unit": "trials/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": trial[0] - args.steps - 1, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
+           "dtype": "f32 neurons, f64 weights", "data": "synthetic (seeded networks and Philox noise)",
+           "config": {"workload": f"{len(nets)} growing networks, HVC-RA log-uniform 200-8000 (seed 4), HVC-I = RA/4, "
+                                  "uniform delays 0-w, w in {0,1,3,6,10} ms round-robin; a step is one growth trial "
+                                  "of every network",
+                      "ra_total": int(sum(n.n_ra for n in nets)), "ra_min": int(min(n.n_ra for n in nets)),
+                      "ra_max": int(max(n.n_ra for n in nets))},
+           "neuron_steps_per_s": neurons * (NUM_STEPS - 1) * args.steps / wall,
+           "gpu_launches": launches, "clocks": clk.summary(),
+           "autotune": {"shape": list(tuned["shape"]), "cached": tuned["cached"], "rounds": tuned["rounds"],
+                        "table": tuned["table"]},
+           "kernel_ms_per_round": kt}
+    if not args.skip_sequential:
+        # the same trials one network at a time on the single-network path
+        seq = 0.0
+        for rn in rns:
+            rn.run_growth_trials(trial[0], 1, True)   # captures the network's graph
+            eng.synchronize()
+            t0 = time.perf_counter()
+            rn.run_growth_trials(trial[0] + 1, 1, True)
+            eng.synchronize()
+            seq += time.perf_counter() - t0
+        res["one_network_at_a_time"] = {"s_per_round": seq, "group_speedup": seq / (wall / args.steps)}
+    if not args.skip_fp64:
+        order = sorted(range(len(nets)), key=lambda k: nets[k].n_ra)
+        pick = [order[0], order[len(order) // 2], order[-1]]
+        secs = _fp64_plain_seconds([nets[k] for k in pick], local_rank, "growth")
+        est = sum(_interp_loglog([nets[k].n_ra for k in pick], secs, n.n_ra) for n in nets)
+        res["fp64_plain_gpu"] = {"sampled_networks_ra": [nets[k].n_ra for k in pick], "s_per_trial": secs,
+                                 "est_s_per_round": est, "est_speedup_of_value": est / (wall / args.steps),
+                                 "how": "double precision, one network and one trial at a time, no graph; the "
+                                        "round time is interpolated (log-log in HVC-RA count) from 3 sampled networks"}
+    for rn in rns:
+        rn.free()
+    eng.close()
+    return res
+
+
+def run_serve(args, local_rank):
+    """Serving: growth and test-trial requests of mixed network size arrive as a
+    Poisson stream; the engine's scheduler admits them by device footprint into the
+    running group rounds.  Reports latency percentiles and trials/s."""
+    import numpy as np
+
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    from unsupervised_growth_gb300.workloads import request_stream
+    B.build()
+    reqs = request_stream(n_requests=args.requests, rate_hz=args.rate)
+    nets = [r.network() for r in reqs]
+    eng = Engine(precision=32, device=local_rank)
+    eng.server_start(max_members=args.members)
+    # warm-up: one small request of each kind (graph capture of both group graphs)
+    for kind in ("growth", "test"):
+        w = reqs[0].__class__(0.0, kind, 300, 2, 7)
+        info = eng.poll(eng.submit(w.network(), kind, 0, 2, True), 300.0)
+        eng.adopt(w.network(), info["net_id"], kind, 2).free()
+    ids = [None] * len(reqs)
+    t_start = time.perf_counter()
+
+    def submitter():
+        for k, (r, net) in enumerate(zip(reqs, nets)):
+            delay = t_start + r.arrival - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids[k] = eng.submit(net, r.kind, 0, r.n_trials, True)
+
+    th = threading.Thread(target=submitter)
+    with ClockSampler(local_rank) as clk:
+        th.start()
+        infos = [None] * len(reqs)
+        pending = set(range(len(reqs)))
+        while pending:
+            for k in list(pending):
+                if ids[k] is None:
+                    continue
+                info = eng.poll(ids[k])
+                if info["state"] in ("done", "failed"):
+                    infos[k] = info
+                    pending.discard(k)
+                    if info["net_id"] >= 0:
+                        eng.adopt(nets[k], info["net_id"], reqs[k].kind, reqs[k].n_trials).free()
+            time.sleep(0.002)
+        th.join()
+    eng.server_stop()
+    failed = [i for i in infos if i["state"] != "done"]
+    lat = np.array([i["t_done"] - i["t_submit"] for i in infos])
+    wait = np.array([i["t_admit"] - i["t_submit"] for i in infos])
+    t0 = min(i["t_submit"] for i in infos)
+    t1 = max(i["t_done"] for i in infos)
+    trials = sum(r.n_trials for r in reqs)
+    nsteps = sum(r.n_trials * (r.n_ra + max(r.n_ra // 4, 1)) * (NUM_STEPS - 1) for r in reqs)
+    res = {"metric": "served trials/s and request latency (Poisson stream of growth and test-trial requests)",
+           "value": trials / (t1 - t0), "unit": "trials/s", "n_gpus": 1, "steps": len(reqs), "warmup": 2,
+           "ms_per_step": 1e3 * (t1 - t0) / len(reqs), "higher_is_better": True, "dtype": "f32 neurons, f64 weights",
+           "data": "synthetic (seeded request stream, networks and Philox noise)",
+           "config": {"workload": f"{len(reqs)} requests, Poisson arrivals at {args.rate}/s, HVC-RA log-uniform "
+                                  "200-8000, HVC-I = RA/4, 1-50 trials per request, growth or test with p = 0.5",
+                      "trials": trials, "max_members": args.members},
+           "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                         "max": float(lat.max())},
+           "queue_wait_s": {"p50": float(np.percentile(wait, 50)), "p99": float(np.percentile(wait, 99))},
+           "neuron_steps_per_s": nsteps / (t1 - t0), "failed": len(failed), "clocks": clk.summary()}
+    if not args.skip_fp64:
+        est = 0.0
+        sample = {}
+        for kind in ("growth", "test"):
+            sizes = [r.n_ra for r in reqs if r.kind == kind]
+            if not sizes:
+                continue
+            pick = sorted({min(sizes), int(np.median(sizes)), max(sizes)})
+            from unsupervised_growth_gb300.workloads import Request
+            secs = _fp64_plain_seconds([Request(0.0, kind, n, 1, 99).network() for n in pick], local_rank, kind)
+            sample[kind] = {"ra": pick, "s_per_trial": secs}
+            est += sum(r.n_trials * _interp_loglog(pick, secs, r.n_ra) for r in reqs if r.kind == kind)
+        res["fp64_plain_serial"] = {"est_seconds": est, "est_trials_per_s": trials / est,
+                                    "speedup_of_value": (trials / (t1 - t0)) / (trials / est), "sample": sample,
+                                    "how": "every request alone, one trial at a time, double precision, no graph; "
+                                           "per-trial times interpolated (log-log in HVC-RA count) from sampled sizes"}
+    eng.close()
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -385,8 +582,14 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="test", choices=["test", "growth"],
-                    help="test: batched test trials (the headline); growth: consecutive growth trials of one network")
+    ap.add_argument("--workload", default="test", choices=["test", "growth", "uneven", "serve"],
+                    help="test: batched test trials (the headline); growth: consecutive growth trials of one "
+                         "network; uneven: one group of growing networks of uneven size; serve: a Poisson stream "
+                         "of requests through the serving loop")
+    ap.add_argument("--members", type=int, default=64, help="uneven: networks in the group; serve: member slots")
+    ap.add_argument("--requests", type=int, default=48, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")
+    ap.add_argument("--skip-sequential", action="store_true", help="uneven: skip the one-network-at-a-time timing")
     ap.add_argument("--batch", type=int, default=BATCH, help="test trials per step (profiling runs use fewer)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
@@ -399,6 +602,10 @@ def main():
         res = run_reference(args, rank)
     elif args.workload == "growth":
         res = run_growth(args, local_rank) if rank == 0 else None
+    elif args.workload == "uneven":
+        res = run_uneven(args, local_rank) if rank == 0 else None
+    elif args.workload == "serve":
+        res = run_serve(args, local_rank) if rank == 0 else None
     else:
         res = run_ours(args, rank, world, local_rank)
     if rank == 0 and res is not None:

@@ -147,9 +147,11 @@ typedef struct {
  * num_steps and appear once each.  Returns the first failing status (UG_OK if none); the
  * items' status fields say which failed, and a failed item drops out of later rounds. */
 ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items);
-/* Caps the blocks per SM of the group launches of the two integrators (0: the occupancy
- * limit).  The autotuner's knob. */
-ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm);
+/* Launch shape of group runs and of the serving loop, the autotuner's knobs: the blocks per
+ * SM of the two integrators' persistent grids (0: the occupancy limit), and whether the
+ * interneuron kernel runs beside the HVC(RA) kernel on a second stream (overlap 1) or after
+ * it (0).  Results do not depend on the shape. */
+ug_status ug_set_group_launch(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm, int32_t overlap);
 /* Serving loop -- no counterpart in the reference.  A scheduler thread of the context
  * runs group rounds (see ug_run_group) over the requests on the GPU and, between
  * rounds, admits queued requests in arrival order while their device footprint fits

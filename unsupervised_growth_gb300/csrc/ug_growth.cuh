@@ -58,6 +58,7 @@ struct GrowthDev {
     uint8_t* pre_cnt;       // [B][n][n] events delivered so far (saturates at 255)
     int* post_step;         // [B][n][kPostRing] sync steps of post events, ring
     int* post_cnt;          // [B][n]
+    double* post_last;      // [B][n] time of the newest post event (-1e300: none this trial)
     int* st_step;           // [B][n][kMaxStreams] spike step of each live stream
     int* st_cursor;         // [B][n][kMaxStreams]
     int* st_len;            // [B][n][kMaxStreams] targets in the stream (n-1, or the snapshot size)
@@ -414,79 +415,135 @@ __device__ __forceinline__ bool g_rank(RowShared& sh, int total, int nrun, int l
     return sorted;
 }
 
-// Processes the ranked events of row i, 32 at a time.  An event is delivered
-// at the first step whose time reaches its delivery time.  Events that cannot
-// change the row's state commit in parallel; the first one that can (or a
-// target seen twice in the chunk) goes through g_deliver alone.
+// One ranked event of row i as seen by the fast path: what it would do to its
+// own pair, and whether that could change the row (an activation,
+// deactivation or supersynapse change -- which is also the only way the row
+// desaturates).
+struct RowEv {
+    bool has, changing, is_active, do_write, new_pre;
+    int t, spk, pc, sd;
+    size_t ij;
+    double wv, w2;
+};
+
+template <class R>
+__device__ __forceinline__ void g_eval(const GrowthDev& g, const NetDev<R>& n, int b, int i, int sa,
+                                       const double* Tseg, const RowShared& sh, int e, int total, int rem, int sc,
+                                       RowEv& v)
+{
+    const SynParams& sp = g.sp;
+    v.has = e < total;
+    v.changing = v.do_write = v.new_pre = v.is_active = false;
+    v.t = -1;
+    v.wv = v.w2 = 0.0;
+    v.pc = v.spk = 0;
+    v.sd = sa;
+    v.ij = 0;
+    if (!v.has) return;
+    const double td = sh.td[1][e];
+    v.t = sh.tgt[1][e];
+    v.spk = sh.spk[1][e];
+    while (Tseg[v.sd - sa] < td) ++v.sd;
+    v.ij = gidx(g, b, i, v.t);
+    // loads of the pair and the target, issued together
+    const int act = g.active[v.ij];
+    const int su = g.super[v.ij];
+    v.wv = g.W[v.ij];
+    v.pc = g.pre_cnt[v.ij];
+    const int ls = g.pre_step[v.ij * kPreRing + ((v.pc + kPreRing - 1) % kPreRing)];
+    const double plast = g.post_last[(size_t)b * g.n + v.t];
+    const double Dij = g.D[v.ij];
+    v.is_active = act == 1;
+    // new pre-synaptic event: first, or more than 30 ms after the previous one
+    v.new_pre = v.pc == 0 || td > n.T[v.pc ? ls : 0] + Dij + 30.0;
+    v.w2 = v.wv;
+    const double now = Tseg[v.sd - sa];
+    // LTD against the target's post events in [now - 100, now]; none when the newest is older
+    if (v.new_pre && (sc != sp.Nss || su == 1) && plast >= now - 100.0) {
+        const int np = post_num(g, b, v.t);
+        for (int k = 0; k < np; ++k) {
+            const double tp = n.T[post_at(g, b, v.t, k)];
+            if (!(tp >= now - 100.0)) continue;
+            g_LTD(sp, v.w2, tp - td);
+            v.do_write = true;
+            v.changing |= (v.w2 >= sp.ACTIVATION_THRESHOLD && !v.is_active && rem == 0) ||
+                          (v.w2 >= sp.SUPERSYNAPSE_THRESHOLD && su == 0 && sc < sp.Nss) ||
+                          (v.w2 < sp.SUPERSYNAPSE_THRESHOLD && su == 1) ||
+                          (v.w2 < sp.ACTIVATION_THRESHOLD && v.is_active);
+        }
+    }
+}
+
+template <class R>
+__device__ __forceinline__ void g_commit(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b,
+                                         const RowEv& v)
+{
+    if (v.is_active) {
+        // update_Ge_RA[target] += w, applied at the sync closing the delivery step
+        const size_t slot = (size_t)(n.syncidx[v.sd] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + v.t;
+        atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(v.wv * kFixScale));
+    }
+    if (v.new_pre) {
+        g.pre_step[v.ij * kPreRing + (v.pc % kPreRing)] = (short)v.spk;
+        if (v.pc < 252) g.pre_cnt[v.ij] = (uint8_t)(v.pc + 1);
+        else atomicOr(g.error, kErrEventCapacity);
+    }
+    if (v.do_write) g.W[v.ij] = v.w2;
+}
+
+constexpr int kEvPerLane = 4;   // events a lane evaluates per chunk (their loads overlap)
+
+// Processes the ranked events of row i in chunks of up to 128.  An event is
+// delivered at the first step whose time reaches its delivery time.  Events
+// that cannot change the row's state touch only their own pair and commit in
+// parallel; the first one that can goes through g_deliver alone, and the
+// chunk restarts after it.  A chunk mixing events of several spikes may hold a
+// target twice: it is cut to 32 events and the repeats take the exact path.
 template <class R>
 __device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
                                           size_t r, int sa, const double* Tseg, int total, const RowShared& sh,
                                           int lane)
 {
-    const SynParams& sp = g.sp;
     int base = 0;
     while (base < total) {
-        const int e = base + lane;
-        const bool has = e < total;
         const int rem = g.remodeled[r];
         const int sc = g.sup_cnt[r];
-        const bool sat = sc == sp.Nss;
-        bool changing = false, do_write = false, new_pre = false, is_active = false;
-        double wv = 0.0, w2 = 0.0, td = 0.0;
-        int t = -1, spk = 0, pc = 0, sd = sa;
-        size_t ij = 0;
-        if (has) {
-            td = sh.td[1][e];
-            t = sh.tgt[1][e];
-            spk = sh.spk[1][e];
-            while (Tseg[sd - sa] < td) ++sd;
-            ij = gidx(g, b, i, t);
-            is_active = g.active[ij] == 1;
-            const bool su = g.super[ij] == 1;
-            wv = g.W[ij];
-            pc = g.pre_cnt[ij];
-            if (pc == 0) {
-                new_pre = true;
-            } else {
-                const int last = g.pre_step[ij * kPreRing + ((pc - 1) % kPreRing)];
-                new_pre = td > n.T[last] + g.D[ij] + 30.0;
-            }
-            w2 = wv;
-            if (new_pre && (!sat || su)) {
-                const double now = Tseg[sd - sa];
-                const int np = post_num(g, b, t);
-                for (int k = 0; k < np; ++k) {
-                    const double tp = n.T[post_at(g, b, t, k)];
-                    if (!(tp >= now - 100.0)) continue;
-                    g_LTD(sp, w2, tp - td);
-                    do_write = true;
-                    changing |= (w2 >= sp.ACTIVATION_THRESHOLD && !is_active && rem == 0) ||
-                                (w2 >= sp.SUPERSYNAPSE_THRESHOLD && !su && sc < sp.Nss) ||
-                                (w2 < sp.SUPERSYNAPSE_THRESHOLD && su) ||
-                                (w2 < sp.ACTIVATION_THRESHOLD && is_active);
-                }
-            }
-            const unsigned same = __match_any_sync(__activemask(), t);
-            if (__popc(same) > 1 && lane != __ffs(same) - 1) changing = true;
+        const int spk0 = sh.spk[1][base];
+        bool one = true;
+#pragma unroll
+        for (int k = 0; k < kEvPerLane; ++k) {
+            const int e = base + k * 32 + lane;
+            if (e < total && sh.spk[1][e] != spk0) one = false;
         }
-        const unsigned chg = __ballot_sync(0xffffffffu, has && changing);
-        const int nchunk = min(32, total - base);
-        const int f = chg ? __ffs(chg) - 1 : nchunk;
-        if (has && lane < f) {
-            if (is_active) {
-                const size_t slot = (size_t)(n.syncidx[sd] % n.ring) * bt.B * n.n_ra + (size_t)b * n.n_ra + t;
-                atomicAdd((unsigned long long*)&bt.ring_ra_exc[slot], (unsigned long long)llrint(wv * kFixScale));
-            }
-            if (new_pre) {
-                g.pre_step[ij * kPreRing + (pc % kPreRing)] = (short)spk;
-                if (pc < 252) g.pre_cnt[ij] = (uint8_t)(pc + 1);
-                else atomicOr(g.error, kErrEventCapacity);
-            }
-            if (do_write) g.W[ij] = w2;
+        const int slices = __all_sync(0xffffffffu, one) ? kEvPerLane : 1;
+        RowEv v[kEvPerLane];
+#pragma unroll
+        for (int k = 0; k < kEvPerLane; ++k)
+            g_eval(g, n, b, i, sa, Tseg, sh, k < slices ? base + k * 32 + lane : total, total, rem, sc, v[k]);
+        if (slices == 1) {
+            const unsigned same = __match_any_sync(0xffffffffu, v[0].has ? v[0].t : -1 - lane);
+            if (v[0].has && __popc(same) > 1 && lane != __ffs(same) - 1) v[0].changing = true;
         }
+        const int nchunk = min(slices * 32, total - base);
+        int f = nchunk;
+#pragma unroll
+        for (int k = kEvPerLane - 1; k >= 0; --k) {
+            const unsigned m = __ballot_sync(0xffffffffu, v[k].has && v[k].changing);
+            if (m) f = k * 32 + __ffs(m) - 1;
+        }
+        f = min(f, nchunk);
+#pragma unroll
+        for (int k = 0; k < kEvPerLane; ++k)
+            if (v[k].has && k * 32 + lane < f) g_commit(g, n, bt, b, v[k]);
         __syncwarp();
         if (f < nchunk) {
-            const int sdf = __shfl_sync(0xffffffffu, sd, f);
+            const int kf = f >> 5, lf = f & 31;
+            int sdf = 0;
+#pragma unroll
+            for (int k = 0; k < kEvPerLane; ++k) {
+                const int x = __shfl_sync(0xffffffffu, v[k].sd, lf);
+                if (k == kf) sdf = x;
+            }
             if (lane == 0) g_deliver(g, n, bt, b, i, sh.tgt[1][base + f], sdf, sh.spk[1][base + f], sh.td[1][base + f]);
             __syncwarp();
             base += f + 1;
@@ -496,15 +553,6 @@ __device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n
     }
 }
 
-// Row i's deliveries over steps s0..s1, one warp per row.  The interval is cut
-// at row i's own spikes (a spike opens a stream whose saturated snapshot
-// depends on the deliveries before it).  Within a segment [sa, sb] the
-// reference delivers, step by step, every event due at that step in (time,
-// target) order; since the delivery step rises with the delivery time, that
-// is the (time, target, spike) order of all events due by T[sb], which the
-// warp gathers and ranks once per segment.  A segment whose events overflow
-// the buffer is replayed step by step, and a step that still overflows is
-// drained one event at a time.
 // One warp, row i of instance b; sh_T holds T[s0..s1].  Returns the row's
 // live streams after the interval.
 template <class R>
@@ -697,6 +745,7 @@ __device__ __forceinline__ void g_newpost_body(const GrowthDev& g, const NetDev<
             const size_t rj = (size_t)b * g.n + j;
             g.post_step[rj * kPostRing + (g.post_cnt[rj] % kPostRing)] = s1;
             g.post_cnt[rj] += 1;
+            g.post_last[rj] = n.T[s1];
         }
     }
 }
@@ -787,6 +836,7 @@ __device__ __forceinline__ void g_reset_body(const GrowthDev& g, int part, int n
     for (size_t k = tid; k < npair; k += (size_t)nparts * blockDim.x) g.pre_cnt[k] = 0;
     for (size_t k = tid; k < nr; k += (size_t)nparts * blockDim.x) {
         g.post_cnt[k] = 0;
+        g.post_last[k] = -1e300;
         g.st_head[k] = 0;
         g.st_num[k] = 0;
         if (g.row_stamp) g.row_stamp[k] = 0;

@@ -275,7 +275,7 @@ private:
     bool rara_dirty_ = false;       // device synapse lists changed since the static lists were built
     ug::GrowthDev gd_{};
     DevMem gW_, gD_, gPerm_, gActive_, gSuper_, gActList_, gActCnt_, gSupList_, gSupCnt_, gRemod_, gPreStep_,
-        gPreCnt_, gPostStep_, gPostCnt_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
+        gPreCnt_, gPostStep_, gPostCnt_, gPostLast_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
         gNewpostCnt_, gSomaBits_, gBad_, gRep_, gStamp_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
@@ -615,7 +615,7 @@ size_t NetImpl<R>::device_bytes() const
                             &mean_inj_})
         t += m->bytes();
     for (const DevMem* m : {&gW_, &gD_, &gPerm_, &gActive_, &gSuper_, &gActList_, &gActCnt_, &gSupList_, &gSupCnt_,
-                            &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gStStep_, &gStCur_, &gStLen_,
+                            &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gPostLast_, &gStStep_, &gStCur_, &gStLen_,
                             &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_,
                             &gStamp_})
         t += m->bytes();
@@ -639,7 +639,7 @@ size_t NetImpl<R>::footprint(int kind, int B) const
     t += (size_t)ring * 8 * (2 * bra + bi) + (size_t)B * (cap * 8 + 16);
     if (kind == 1) {
         const size_t nn = nra * nra;
-        t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 3 * 4 * ug::kMaxStreams +
+        t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 8 + 3 * 4 * ug::kMaxStreams +
                               4 * ug::kMaxStreams * ug::kMaxNss + 8 + 64 + 4 + 4 + 4) + 8;
     }
     return t;
@@ -788,6 +788,7 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     UG_TRY(gPreCnt_.alloc(nn));
     UG_TRY(gPostStep_.alloc((size_t)n * ug::kPostRing * sizeof(int)));
     UG_TRY(gPostCnt_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gPostLast_.alloc((size_t)n * sizeof(double)));
     UG_TRY(gStStep_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
     UG_TRY(gStCur_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
     UG_TRY(gStLen_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
@@ -812,7 +813,7 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     g.act_list = gActList_.as<int>(); g.act_cnt = gActCnt_.as<int>();
     g.sup_list = gSupList_.as<int>(); g.sup_cnt = gSupCnt_.as<int>(); g.remodeled = gRemod_.as<int>();
     g.pre_step = gPreStep_.as<short>(); g.pre_cnt = gPreCnt_.as<uint8_t>();
-    g.post_step = gPostStep_.as<int>(); g.post_cnt = gPostCnt_.as<int>();
+    g.post_step = gPostStep_.as<int>(); g.post_cnt = gPostCnt_.as<int>(); g.post_last = gPostLast_.as<double>();
     g.st_step = gStStep_.as<int>(); g.st_cursor = gStCur_.as<int>(); g.st_len = gStLen_.as<int>();
     g.st_tgt = gStTgt_.as<int>(); g.st_head = gStHead_.as<int>(); g.st_num = gStNum_.as<int>();
     g.newpost = gNewpost_.as<int>(); g.newpost_cnt = gNewpostCnt_.as<int>();
@@ -1218,7 +1219,7 @@ class GroupExec : public GroupBase {
 public:
     ~GroupExec() override { drop_graphs(); }
     ug_status run_round(std::vector<RoundItem<R>>& items, const ug::LaunchCtx& lc, bool graphs, int ra_bps,
-                        int i_bps, int64_t* launches);
+                        int i_bps, int overlap, int64_t* launches);
 
 private:
     void drop_graphs()
@@ -1250,7 +1251,7 @@ private:
 
 template <class R>
 ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::LaunchCtx& lc, bool graphs,
-                                  int ra_bps, int i_bps, int64_t* launches)
+                                  int ra_bps, int i_bps, int overlap, int64_t* launches)
 {
     cudaStream_t st = lc.main;
     if (items.empty()) return UG_OK;
@@ -1273,10 +1274,11 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
         num_steps_ = num_steps;
         drop_graphs();
     }
-    if (ra_bps != ra_bps_ || i_bps != i_bps_) {
+    if (ra_bps != ra_bps_ || i_bps != i_bps_ || overlap != dev_.fork) {
         UG_CUDA(ug::group_grids<R>(dev_, ra_bps, i_bps));
         ra_bps_ = ra_bps;
         i_bps_ = i_bps;
+        dev_.fork = overlap;
         drop_graphs();
     }
     // per-member preparation (uploads of trial indices and injection times)
@@ -1422,6 +1424,7 @@ struct ug_ctx {
     std::map<int, std::unique_ptr<NetBase>> nets;
     std::unique_ptr<GroupBase> group;          // GroupExec<float> or GroupExec<double>
     int group_ra_bps = 0, group_i_bps = 0;     // integrator blocks per SM of group launches (0: occupancy)
+    int group_overlap = 1;                     // interneuron kernel beside the RA kernel
     std::recursive_mutex mu;                   // one caller at a time: API calls and the server's rounds
     std::unique_ptr<Server> server;
     ~ug_ctx();
@@ -1666,7 +1669,7 @@ void Server::round()
         else items.push_back({n, 1, r->first_trial + (uint32_t)r->trials_done, 1, r->training, UG_OK});
     }
     const ug_status s = ge->run_round(items, ctx_->launch_ctx(), ctx_->graphs, ctx_->group_ra_bps, ctx_->group_i_bps,
-                                      &ctx_->launches);
+                                      ctx_->group_overlap, &ctx_->launches);
     const std::string msg = g_err;
     const double t = now_s();
     bool attributed = false;
@@ -1725,7 +1728,7 @@ ug_status run_group_typed(ug_ctx* ctx, ug_group_item* items, int n_items)
         }
         if (round.empty()) break;
         const ug_status s = ge->run_round(round, ctx->launch_ctx(), ctx->graphs, ctx->group_ra_bps,
-                                          ctx->group_i_bps, &ctx->launches);
+                                          ctx->group_i_bps, ctx->group_overlap, &ctx->launches);
         bool attributed = false;
         for (size_t j = 0; j < round.size(); ++j) {
             items[idx[j]].status = round[j].status;
@@ -1879,7 +1882,7 @@ ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items)
                                 : run_group_typed<float>(ctx, items, n_items);
 }
 
-ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm)
+ug_status ug_set_group_launch(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm, int32_t overlap)
 {
     if (!ctx) return fail(UG_EINVAL, "null context");
     std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
@@ -1887,6 +1890,7 @@ ug_status ug_set_group_grid(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blo
     if (ra_blocks_per_sm < 0 || i_blocks_per_sm < 0) return fail(UG_EINVAL, "blocks per SM must be >= 0");
     ctx->group_ra_bps = ra_blocks_per_sm;
     ctx->group_i_bps = i_blocks_per_sm;
+    ctx->group_overlap = overlap ? 1 : 0;
     return UG_OK;
 }
 

@@ -197,7 +197,7 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
         UG_TIMED(lc, "k_growth_reset", (kl_growth_reset<R><<<d.grid[kListReset], 256, 0, lc.main>>>(mem, d.items[kListReset], c + kListReset)));
         ++cnt;
     }
-    const bool fork = !lc.timer && lc.side && lc.side != lc.main;
+    const bool fork = d.fork && !lc.timer && lc.side && lc.side != lc.main;
     const int Q = (int)sync_steps.size();
     for (int q = 0; q <= Q; ++q) {
         const int s0 = q == 0 ? 1 : (q < Q ? sync_steps[q - 1] + 1 : num_steps);

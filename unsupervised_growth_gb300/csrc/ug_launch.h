@@ -127,6 +127,7 @@ struct GroupDev {
     int* bad = nullptr;                       // [members] check_bad_values flags
     const double* T = nullptr;                // the group's time grid
     int grid[kNumLists + 1] = {};             // blocks of each list kernel; [kNumLists] = row kernel
+    int fork = 1;                             // interneuron kernel on the side stream, beside the RA kernel
 };
 
 // Occupancy-sized grids of the list kernels (call outside stream capture);

@@ -23,7 +23,7 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
-            "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_grid",
+            "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_launch",
             "ug_server_start", "ug_submit", "ug_poll", "ug_server_stop", "ug_get_weights", "ug_get_delays",
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
@@ -129,7 +129,7 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_trial_stats.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p]
     L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
     L.ug_run_group.argtypes = [vp, C.POINTER(GroupItem), C.c_int32]
-    L.ug_set_group_grid.argtypes = [vp, C.c_int32, C.c_int32]
+    L.ug_set_group_launch.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     L.ug_server_start.argtypes = [vp, C.POINTER(ServerOpts)]
     L.ug_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
     L.ug_poll.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]
@@ -325,8 +325,9 @@ class Engine:
         _check(st)
         return statuses
 
-    def set_group_grid(self, ra_blocks_per_sm: int = 0, i_blocks_per_sm: int = 0):
-        _check(self.L.ug_set_group_grid(self.ctx, ra_blocks_per_sm, i_blocks_per_sm))
+    def set_group_launch(self, ra_blocks_per_sm: int = 0, i_blocks_per_sm: int = 0, overlap: bool = True):
+        """Launch shape of group runs and of the serving loop (the autotuner's knobs)."""
+        _check(self.L.ug_set_group_launch(self.ctx, ra_blocks_per_sm, i_blocks_per_sm, 1 if overlap else 0))
 
     # ---- serving loop
     def server_start(self, hbm_budget_bytes: int = 0, max_members: int = 0):
