@@ -424,8 +424,9 @@ def run_uneven(args, local_rank):
     launches = eng.launch_count() - l0
     eng.set_kernel_timing(True)
     one_round()
-    names = ("k_trial_init", "k_noise_events", "k_growth_reset", "k_interval_ra", "k_interval_i", "k_growth_rows",
-             "k_growth_newpost", "k_growth_ltp", "k_growth_epilogue", "k_check_bad")
+    names = ("k_trial_init", "k_noise_events", "k_growth_reset", "k_interval_ra", "k_interval_i",
+             "k_growth_rows_heavy", "k_growth_rows", "k_growth_newpost", "k_growth_ltp", "k_growth_epilogue",
+             "k_check_bad")
     kt = {k: round(eng.kernel_timing(k)[0], 3) for k in names}
     eng.set_kernel_timing(False)
     neurons = sum(n.n_ra + n.n_i for n in nets)

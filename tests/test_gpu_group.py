@@ -93,3 +93,34 @@ def test_group_of_test_batches_then_regroup(engine32):
         for rn, (kind, _, _, _), ref in zip(rns, mix, alone):
             _assert_same(_state(rn, kind), ref, kind)
             rn.free()
+
+
+def heavy_growth(seed, width, delays="uniform"):
+    """A network large enough (>= 1024 HVC-RA) for spiking rows to take the block path."""
+    net = small_growth(seed=seed, n_ra=1100, n_i=275, n_tr=10, syn=SYN, mat=MAT, delays=delays, delay_width=width)
+    net.training_spread = np.linspace(0.0, 5.0, len(net.training))
+    net.trials_after_replacement[net.training] = 0
+    return net
+
+
+HEAVY = [
+    ("growth", lambda: heavy_growth(41, 0.0), 0, 2),
+    ("growth", lambda: heavy_growth(42, 0.5), 0, 2),
+    ("growth", lambda: heavy_growth(43, 0.0, delays="lognormal"), 0, 2),
+    ("test", lambda: small_chain(seed=5), 0, 4),
+]
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_group_heavy_rows_match_single_networks(precision, engine32, engine64):
+    """Spiking rows of networks of 1024 HVC-RA or more take the block-per-row path in
+    a group; the single-network path walks every row with one warp.  Same results."""
+    eng = engine32 if precision == 32 else engine64
+    mix = HEAVY if precision == 32 else HEAVY[:2]
+    alone = _alone(eng, mix)
+    rns = [eng.load_network(mk()) for _, mk, _, _ in mix]
+    status = eng.run_group([(rn, kind, first, n, True) for rn, (kind, _, first, n) in zip(rns, mix)])
+    assert status == ["UG_OK"] * len(mix)
+    for rn, (kind, _, _, _), ref in zip(rns, mix, alone):
+        _assert_same(_state(rn, kind), ref, kind)
+        rn.free()

@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? UG_RA_MIN_BLOCKS : 1)
                    int s1)
 {
     __shared__ GroupMember<R> M;
-    if (act_cnt && blockIdx.x == 0 && threadIdx.x == 0) act_cnt[(q + 1) & 1] = 0;
+    if (act_cnt && blockIdx.x == 0 && threadIdx.x == 0) {
+        act_cnt[(q + 1) & 1] = 0;       // the next interval's queues, read by the
+        act_cnt[2 + ((q + 1) & 1)] = 0; // row kernels of the previous one
+    }
     for_items(members, items, *count, M, [&](const GroupMember<R>& m, int bx, int by) {
         if constexpr (sizeof(R) == 4) interval_ra_x2_body(m.n, m.bt, q, s0, s1, m.rc, bx, by);
         else interval_ra_body(m.n, m.bt, q, s0, s1, m.rc, bx, by);
@@ -115,8 +118,7 @@ __global__ void __launch_bounds__(256) kl_growth_reset(const GroupMember<R>* mem
               [](const GroupMember<R>& m, int part, int nparts) { g_reset_body(m.g, part, nparts); });
 }
 
-// One warp per queued row of interval q; rows whose streams stay open are
-// queued again for interval q + 1.  T = the group's time grid.
+// One warp per queued row of interval q (the warp path).  T = the group's time grid.
 template <class R>
 __global__ void __launch_bounds__(32 * kRowWarps) kl_growth_rows(const GroupMember<R>* members, const int2* rows,
                                                                  const int* act_cnt, int act_cap, const double* T,
@@ -142,9 +144,39 @@ __global__ void __launch_bounds__(32 * kRowWarps) kl_growth_rows(const GroupMemb
         }
         const GroupMember<R>& m = M[w];
         const int b = it.y / m.n.n_ra, i = it.y - b * m.n.n_ra;
-        const int num = g_row(m.g, m.n, m.bt, b, i, s0, s1, sh_T, sh, lane);
-        if (num > 0 && lane == 0) queue_row(m.bt, q + 1, it.y);
+        g_row(m.g, m.n, m.bt, b, i, s0, s1, sh_T, sh, lane);
         __syncwarp();
+    }
+}
+
+// One block per queued heavy row of interval q (spiking rows of large networks).
+template <class R>
+__global__ void __launch_bounds__(32 * kHeavyWarps) kl_growth_rows_heavy(const GroupMember<R>* members,
+                                                                         const int2* rows, const int* act_cnt,
+                                                                         int act_cap, const double* T, int q, int s0,
+                                                                         int s1)
+{
+    extern __shared__ __align__(16) unsigned char heavy_smem[];
+    __shared__ double sh_T[kSegSteps];
+    __shared__ GroupMember<R> M;
+    for (int k = threadIdx.x; k <= s1 - s0 && k < kSegSteps; k += blockDim.x) sh_T[k] = T[s0 + k];
+    __syncthreads();
+    if (s1 - s0 >= kSegSteps) return;
+    RowShared& sh = *reinterpret_cast<RowShared*>(heavy_smem);
+    HeavyShared& hs = *reinterpret_cast<HeavyShared*>(heavy_smem + sizeof(RowShared));
+    const int list = 2 + (q & 1);
+    const int nrows = min(act_cnt[list], act_cap);
+    int cur = -1;
+    for (int e = blockIdx.x; e < nrows; e += gridDim.x) {
+        const int2 it = rows[(size_t)list * act_cap + e];
+        if (it.x != cur) {
+            __syncthreads();
+            copy_words(M, members[it.x], threadIdx.x, blockDim.x);
+            __syncthreads();
+            cur = it.x;
+        }
+        const int b = it.y / M.n.n_ra, i = it.y - b * M.n.n_ra;
+        g_row_heavy(M.g, M.n, M.bt, b, i, s0, s1, sh_T, sh, hs);
     }
 }
 

@@ -68,7 +68,6 @@ struct GrowthDev {
     int* newpost;           // [B][n * 16] new post events of the interval, in order
     int* newpost_cnt;       // [B]
     int* error;
-    int* row_stamp;         // [B][n] interval stamps of the group row queue, or null
 };
 
 __device__ __forceinline__ size_t gidx(const GrowthDev& g, int b, int i, int j)
@@ -426,13 +425,15 @@ struct RowEv {
     double wv, w2;
 };
 
+// Event (td, t, spk) of row i, delivered at the first step >= sa (Tseg = T[sa..])
+// whose time reaches td; has = false evaluates nothing.
 template <class R>
-__device__ __forceinline__ void g_eval(const GrowthDev& g, const NetDev<R>& n, int b, int i, int sa,
-                                       const double* Tseg, const RowShared& sh, int e, int total, int rem, int sc,
-                                       RowEv& v)
+__device__ __forceinline__ void g_eval_ev(const GrowthDev& g, const NetDev<R>& n, int b, int i, int sa,
+                                          const double* Tseg, bool has, double td, int t, int spk, int rem, int sc,
+                                          RowEv& v)
 {
     const SynParams& sp = g.sp;
-    v.has = e < total;
+    v.has = has;
     v.changing = v.do_write = v.new_pre = v.is_active = false;
     v.t = -1;
     v.wv = v.w2 = 0.0;
@@ -440,9 +441,8 @@ __device__ __forceinline__ void g_eval(const GrowthDev& g, const NetDev<R>& n, i
     v.sd = sa;
     v.ij = 0;
     if (!v.has) return;
-    const double td = sh.td[1][e];
-    v.t = sh.tgt[1][e];
-    v.spk = sh.spk[1][e];
+    v.t = t;
+    v.spk = spk;
     while (Tseg[v.sd - sa] < td) ++v.sd;
     v.ij = gidx(g, b, i, v.t);
     // loads of the pair and the target, issued together
@@ -472,6 +472,16 @@ __device__ __forceinline__ void g_eval(const GrowthDev& g, const NetDev<R>& n, i
                           (v.w2 < sp.ACTIVATION_THRESHOLD && v.is_active);
         }
     }
+}
+
+template <class R>
+__device__ __forceinline__ void g_eval(const GrowthDev& g, const NetDev<R>& n, int b, int i, int sa,
+                                       const double* Tseg, const RowShared& sh, int e, int total, int rem, int sc,
+                                       RowEv& v)
+{
+    const bool has = e < total;
+    g_eval_ev(g, n, b, i, sa, Tseg, has, has ? sh.td[1][e] : 0.0, has ? sh.tgt[1][e] : -1, has ? sh.spk[1][e] : 0,
+              rem, sc, v);
 }
 
 template <class R>
@@ -553,31 +563,32 @@ __device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n
     }
 }
 
-// One warp, row i of instance b; sh_T holds T[s0..s1].  Returns the row's
-// live streams after the interval.
+// One warp, row i of instance b, steps from..to of the interval s0..s1
+// (sh_T holds T[s0..s1]); a spike at `from` has already opened its stream
+// when opened_at_from is set.  head / num: the row's stream ring.
 template <class R>
-__device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
-                                     int s0, int s1, const double* sh_T, RowShared& sh, int lane)
+__device__ __forceinline__ void g_row_range(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b,
+                                            int i, int s0, int from, int to, bool opened_at_from,
+                                            const double* sh_T, RowShared& sh, int lane, int& head, int& num)
 {
     const size_t r = (size_t)b * g.n + i;
     const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
-    int head = g.st_head[r], num = g.st_num[r];
-    if (bits == 0 && num == 0) return 0;
+    const int s1 = to;
     int* stS = g.st_step + r * kMaxStreams;
     int* stC = g.st_cursor + r * kMaxStreams;
     int* stL = g.st_len + r * kMaxStreams;
     int* stT = g.st_tgt + r * kMaxStreams * kMaxNss;
     const int* perm = g.perm + r * (g.n - 1);
     const double* Drow = g.D + r * g.n;
-    int sa = s0;
+    int sa = from;
     while (sa <= s1) {
-        if ((bits >> (sa - s0)) & 1u) {
+        if (((bits >> (sa - s0)) & 1u) && !(opened_at_from && sa == from)) {
             if (lane == 0) num = g_open_stream(g, r, sa, sh_T[sa - s0], Drow, head, num, stS, stC, stL, stT);
             num = __shfl_sync(0xffffffffu, num, 0);
             __syncwarp();
         }
         const uint32_t later = (sa - s0 + 1) < 32 ? bits >> (sa - s0 + 1) : 0u;
-        const int sb = later ? sa + __ffs(later) - 1 : s1;
+        const int sb = later ? min(sa + __ffs(later) - 1, s1) : s1;
         // Chunks in queue order: gather up to `quota` due events per stream,
         // rank them, and process those no later (in queue order) than the last
         // gathered event of every stream cut at its quota -- no event left
@@ -654,11 +665,197 @@ __device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, con
         __syncwarp();
         sa = sb + 1;
     }
+}
+
+// One warp, row i of instance b over the whole interval s0..s1.  Returns the
+// row's live streams after it.
+template <class R>
+__device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
+                                     int s0, int s1, const double* sh_T, RowShared& sh, int lane)
+{
+    const size_t r = (size_t)b * g.n + i;
+    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    int head = g.st_head[r], num = g.st_num[r];
+    if (bits == 0 && num == 0) return 0;
+    g_row_range(g, n, bt, b, i, s0, s0, s1, false, sh_T, sh, lane, head, num);
     if (lane == 0) {
         g.st_head[r] = head;
         g.st_num[r] = num;
     }
     return num;
+}
+
+// ---------------------------------------------------------------------------
+// Heavy rows: in a large network a spike opens a stream over all n - 1
+// targets, and with short delays thousands of them fall due within one
+// interval.  One warp would walk them 128 at a time; a block of kHeavyWarps
+// warps takes kHeavyChunk of them per pass instead.  The block path applies
+// when exactly one of the row's streams has events due in the rest of the
+// interval and the row does not spike again in it: then the events due are a
+// prefix of that stream, and the stream's (delay, target) order is the
+// queue's (time, target) order wherever that prefix is sorted by (time,
+// target) -- which the block checks pass by pass, handing the row back to the
+// warp path (and its ranked merge) at the first pass that is not.  Everything
+// before a spike of the row, and any remainder, goes through the warp path.
+constexpr int kHeavyWarps = 8;
+constexpr int kHeavyChunk = kHeavyWarps * 32 * kEvPerLane;   // events per block pass
+constexpr int kHeavyMinRows = 1024;                          // networks from this size take the block path
+
+struct HeavyShared {
+    double td[kHeavyChunk];
+    int tgt[kHeavyChunk];
+    double prev_td, Tsp;
+    int prev_t, first, ndue, unsorted, mode, slot, spk, head, num, cur, len, rem, sc;
+};
+
+// Block: queued row i of instance b in the interval s0..s1 (sh_T = T[s0..s1]).
+template <class R>
+__device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b,
+                                            int i, int s0, int s1, const double* sh_T, RowShared& sh,
+                                            HeavyShared& hs)
+{
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t r = (size_t)b * g.n + i;
+    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    const int from = bits ? s0 + __ffs(bits) - 1 : s0;   // the spike, or the interval's start
+    int* stS = g.st_step + r * kMaxStreams;
+    int* stC = g.st_cursor + r * kMaxStreams;
+    int* stL = g.st_len + r * kMaxStreams;
+    int* stT = g.st_tgt + r * kMaxStreams * kMaxNss;
+    const int* perm = g.perm + r * (g.n - 1);
+    const double* Drow = g.D + r * g.n;
+    const double Tlim = sh_T[s1 - s0];
+    if (w == 0) {
+        int head = g.st_head[r], num = g.st_num[r];
+        int mode = 1;
+        if (bits) {
+            if (from > s0 && num > 0) g_row_range(g, n, bt, b, i, s0, s0, from - 1, false, sh_T, sh, lane, head, num);
+            if (lane == 0) {
+                const int before = num;
+                num = g_open_stream(g, r, from, sh_T[from - s0], Drow, head, num, stS, stC, stL, stT);
+                if (num == before || (bits >> (from - s0 + 1)) != 0u) mode = 0;   // no room, or a second spike
+            }
+        }
+        if (lane == 0) {
+            // the one stream with events due by the end of the interval
+            int slot = -1, ndue = 0;
+            for (int q = 0; q < num && mode; ++q) {
+                const int sq = (head + q) % kMaxStreams;
+                const int L = stL[sq];
+                const int len = L < 0 ? -L : L;
+                const int c = stC[sq];
+                if (c >= len) continue;
+                const int t = L < 0 ? stT[sq * kMaxNss + c] : perm[c];
+                if (Tlim >= n.T[stS[sq]] + Drow[t]) {
+                    slot = sq;
+                    ++ndue;
+                }
+            }
+            if (ndue != 1 || stL[slot] <= 0) mode = 0;   // none, several, or a saturated row's snapshot
+            hs.mode = mode;
+            hs.head = head;
+            hs.num = num;
+            if (mode) {
+                hs.slot = slot;
+                hs.spk = stS[slot];
+                hs.Tsp = n.T[stS[slot]];
+                hs.cur = stC[slot];
+                hs.len = stL[slot];
+                hs.prev_td = -1e300;
+                hs.prev_t = -1;
+            }
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    if (hs.mode) {
+        const double Tsp = hs.Tsp;
+        const int spk = hs.spk;
+        const double* Tseg = sh_T + (from - s0);
+        while (true) {
+            if (threadIdx.x == 0) {
+                hs.first = kHeavyChunk;
+                hs.ndue = 0;
+                hs.unsorted = 0;
+                hs.rem = g.remodeled[r];
+                hs.sc = g.sup_cnt[r];
+            }
+            __syncthreads();
+            const int cur = hs.cur, len = hs.len, rem = hs.rem, sc = hs.sc;
+            RowEv v[kEvPerLane];
+            int due_here = 0;
+#pragma unroll
+            for (int k = 0; k < kEvPerLane; ++k) {
+                const int e = w * 32 * kEvPerLane + k * 32 + lane;   // position in the pass
+                const int idx = cur + e;
+                int t = -1;
+                double td = 0.0;
+                bool due = false;
+                if (idx < len) {
+                    t = perm[idx];
+                    td = Tsp + Drow[t];
+                    due = Tlim >= td;
+                }
+                g_eval_ev(g, n, b, i, from, Tseg, due, td, t, spk, rem, sc, v[k]);
+                if (due) {
+                    hs.td[e] = td;
+                    hs.tgt[e] = t;
+                    ++due_here;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, due && v[k].changing);
+                if (m && lane == 0) atomicMin(&hs.first, w * 32 * kEvPerLane + k * 32 + __ffs(m) - 1);
+            }
+            // due events are a prefix of the stream: their count is the prefix length
+            for (int o = 16; o > 0; o >>= 1) due_here += __shfl_xor_sync(0xffffffffu, due_here, o);
+            if (lane == 0) atomicAdd(&hs.ndue, due_here);
+            __syncthreads();
+            const int ndue = hs.ndue;
+            // the prefix must be in (time, target) order, continuing the previous pass
+            for (int e = threadIdx.x; e < ndue; e += blockDim.x) {
+                const double ta = e ? hs.td[e - 1] : hs.prev_td;
+                const int ga = e ? hs.tgt[e - 1] : hs.prev_t;
+                if (!(ta < hs.td[e] || (ta == hs.td[e] && ga < hs.tgt[e]))) hs.unsorted = 1;
+            }
+            __syncthreads();
+            if (hs.unsorted) break;   // the warp path takes over from cur
+            const int f = min(hs.first, ndue);
+#pragma unroll
+            for (int k = 0; k < kEvPerLane; ++k) {
+                const int e = w * 32 * kEvPerLane + k * 32 + lane;
+                if (v[k].has && e < f) g_commit(g, n, bt, b, v[k]);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0 && f < ndue) {
+                // the first event that can change the row: alone, then re-evaluate after it
+                const double tdf = hs.td[f];
+                int sd = from;
+                while (Tseg[sd - from] < tdf) ++sd;
+                g_deliver(g, n, bt, b, i, hs.tgt[f], sd, spk, tdf);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const int adv = f < ndue ? f + 1 : ndue;
+                if (adv > 0) {
+                    hs.prev_td = hs.td[adv - 1];
+                    hs.prev_t = hs.tgt[adv - 1];
+                }
+                hs.cur = cur + adv;
+                stC[hs.slot] = hs.cur;
+            }
+            __syncthreads();
+            if (f >= ndue && ndue < kHeavyChunk) break;
+        }
+    }
+    __syncthreads();
+    if (w == 0) {
+        int head = hs.head, num = hs.num;
+        g_row_range(g, n, bt, b, i, s0, from, s1, bits != 0, sh_T, sh, lane, head, num);
+        if (lane == 0) {
+            g.st_head[r] = head;
+            g.st_num[r] = num;
+        }
+    }
+    __syncthreads();
 }
 
 template <class R>
@@ -839,7 +1036,6 @@ __device__ __forceinline__ void g_reset_body(const GrowthDev& g, int part, int n
         g.post_last[k] = -1e300;
         g.st_head[k] = 0;
         g.st_num[k] = 0;
-        if (g.row_stamp) g.row_stamp[k] = 0;
     }
 }
 

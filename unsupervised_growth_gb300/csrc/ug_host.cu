@@ -276,7 +276,7 @@ private:
     ug::GrowthDev gd_{};
     DevMem gW_, gD_, gPerm_, gActive_, gSuper_, gActList_, gActCnt_, gSupList_, gSupCnt_, gRemod_, gPreStep_,
         gPreCnt_, gPostStep_, gPostCnt_, gPostLast_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
-        gNewpostCnt_, gSomaBits_, gBad_, gRep_, gStamp_;
+        gNewpostCnt_, gSomaBits_, gBad_, gRep_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
     std::vector<int> syncidx_;
@@ -616,8 +616,7 @@ size_t NetImpl<R>::device_bytes() const
         t += m->bytes();
     for (const DevMem* m : {&gW_, &gD_, &gPerm_, &gActive_, &gSuper_, &gActList_, &gActCnt_, &gSupList_, &gSupCnt_,
                             &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gPostLast_, &gStStep_, &gStCur_, &gStLen_,
-                            &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_,
-                            &gStamp_})
+                            &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_})
         t += m->bytes();
     return t;
 }
@@ -936,16 +935,16 @@ ug_status NetImpl<R>::member(ug::GroupMember<R>* m, int index, int2* act_rows, i
     m->bt.member = index;
     m->bt.act_rows = nullptr;
     m->bt.act_cnt = nullptr;
-    m->bt.row_stamp = nullptr;
+    m->bt.live_streams = nullptr;
+    m->bt.heavy = 0;
     m->growth = growth ? 1 : 0;
     if (growth) {
-        if (!gStamp_.as<int>() || gStamp_.bytes() < (size_t)h.n_ra * sizeof(int)) UG_TRY(gStamp_.alloc((size_t)h.n_ra * sizeof(int)));
         m->g = gd_;
-        m->g.row_stamp = gStamp_.as<int>();
         m->bt.act_rows = act_rows;
         m->bt.act_cnt = act_cnt;
         m->bt.act_cap = act_cap;
-        m->bt.row_stamp = gStamp_.as<int>();
+        m->bt.live_streams = gd_.st_num;
+        m->bt.heavy = h.n_ra >= ug::kHeavyMinRows ? 1 : 0;
     }
     return UG_OK;
 }
@@ -1295,11 +1294,11 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
             growth = true;
             rows += it.net->growth_row_count();
         }
-    UG_TRY(reserve(act_rows_, 2 * std::max<size_t>(rows, 1) * sizeof(int2)));
+    UG_TRY(reserve(act_rows_, 4 * std::max<size_t>(rows, 1) * sizeof(int2)));
     // the capacity (not the current row count) is the kernels' bound, so the
     // captured graphs stay valid until the buffer grows
-    const int act_cap = (int)(act_rows_.bytes() / (2 * sizeof(int2)));
-    UG_TRY(reserve(act_cnt_, 2 * sizeof(int)));
+    const int act_cap = (int)(act_rows_.bytes() / (4 * sizeof(int2)));
+    UG_TRY(reserve(act_cnt_, 4 * sizeof(int)));
     UG_TRY(reserve(bad_, items.size() * sizeof(int)));
     UG_TRY(reserve(count_, ug::kNumLists * sizeof(int)));
     // member table and work lists
@@ -1358,7 +1357,7 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
     // launch: one captured graph per kind (with or without growth members),
     // reused across compositions
     const int64_t Q = (int64_t)sync_steps.size();
-    const int64_t n_launch = 2 + (sizeof(R) == 4 ? 1 : 0) + 2 * (Q + 1) + (growth ? 3 * Q + 2 : 0);
+    const int64_t n_launch = 2 + (sizeof(R) == 4 ? 1 : 0) + 2 * (Q + 1) + (growth ? 4 * Q + 2 : 0);
     if (!graphs || lc.timer) {
         UG_CUDA(ug::launch_group_trial<R>(dev_, sync_steps, num_steps, growth, lc, nullptr));
     } else {

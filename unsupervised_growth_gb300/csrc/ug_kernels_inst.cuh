@@ -169,7 +169,8 @@ cudaError_t group_grids(GroupDev& d, int ra_blocks_per_sm, int i_blocks_per_sm)
     d.grid[kListLtp] = occupancy(kl_growth_ltp<R>, kBlock, 0);
     d.grid[kListCheck] = occupancy(kl_check_bad<R>, 256, 0);
     d.grid[kNumLists] = occupancy(kl_growth_rows<R>, 32 * kRowWarps, kRowWarps * sizeof(RowShared));
-    for (int k = 0; k <= kNumLists; ++k)
+    d.grid[kNumLists + 1] = occupancy(kl_growth_rows_heavy<R>, 32 * kHeavyWarps, sizeof(RowShared) + sizeof(HeavyShared));
+    for (int k = 0; k <= kNumLists + 1; ++k)
         if (d.grid[k] <= 0) return cudaErrorInvalidConfiguration;
     return cudaSuccess;
 }
@@ -184,7 +185,7 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
     int64_t cnt = 0;
     cudaError_t e = cudaSuccess;
     if (growth) {
-        e = cudaMemsetAsync(d.act_cnt, 0, 2 * sizeof(int), lc.main);
+        e = cudaMemsetAsync(d.act_cnt, 0, 4 * sizeof(int), lc.main);
         if (e != cudaSuccess) return e;
     }
     UG_TIMED(lc, "k_trial_init", (kl_trial_init<R><<<d.grid[kListInit], kBlock, 0, lc.main>>>(mem, d.items[kListInit], c + kListInit)));
@@ -218,10 +219,23 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
             if (e != cudaSuccess) return e;
         }
         if (growth && q < Q) {
+            // heavy rows (a block each) beside the warp-path rows: different rows, disjoint state
+            const bool rfork = !lc.timer && lc.side && lc.side != lc.main;
+            if (rfork) {
+                e = cudaEventRecord(lc.fork, lc.main);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.side, lc.fork, 0);
+                if (e != cudaSuccess) return e;
+            }
+            UG_TIMED(lc, "k_growth_rows_heavy", (kl_growth_rows_heavy<R><<<d.grid[kNumLists + 1], 32 * kHeavyWarps, sizeof(RowShared) + sizeof(HeavyShared), rfork ? lc.side : lc.main>>>(mem, d.act_rows, d.act_cnt, d.act_cap, d.T, q, s0, s1)));
             UG_TIMED(lc, "k_growth_rows", (kl_growth_rows<R><<<d.grid[kNumLists], 32 * kRowWarps, kRowWarps * sizeof(RowShared), lc.main>>>(mem, d.act_rows, d.act_cnt, d.act_cap, d.T, q, s0, s1)));
+            if (rfork) {
+                e = cudaEventRecord(lc.join, lc.side);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.main, lc.join, 0);
+                if (e != cudaSuccess) return e;
+            }
             UG_TIMED(lc, "k_growth_newpost", (kl_growth_newpost<R><<<d.grid[kListNewpost], 1024, 0, lc.main>>>(mem, d.items[kListNewpost], c + kListNewpost, s0, s1)));
             UG_TIMED(lc, "k_growth_ltp", (kl_growth_ltp<R><<<d.grid[kListLtp], kBlock, 0, lc.main>>>(mem, d.items[kListLtp], c + kListLtp, s1)));
-            cnt += 3;
+            cnt += 4;
         }
     }
     if (growth) {

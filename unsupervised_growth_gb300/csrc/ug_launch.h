@@ -121,12 +121,12 @@ struct GroupDev {
     const void* members = nullptr;            // GroupMember<R>[members]
     const int4* items[kNumLists] = {};
     const int* count = nullptr;               // [kNumLists] items in each list
-    int2* act_rows = nullptr;                 // [2][act_cap] row queue
-    int* act_cnt = nullptr;                   // [2]
+    int2* act_rows = nullptr;                 // [2 paths][2 parities][act_cap] row queues
+    int* act_cnt = nullptr;                   // [4]
     int act_cap = 0;
     int* bad = nullptr;                       // [members] check_bad_values flags
     const double* T = nullptr;                // the group's time grid
-    int grid[kNumLists + 1] = {};             // blocks of each list kernel; [kNumLists] = row kernel
+    int grid[kNumLists + 2] = {};             // blocks of each list kernel; [kNumLists] row kernel, [+1] heavy rows
     int fork = 1;                             // interneuron kernel on the side stream, beside the RA kernel
 };
 

@@ -85,25 +85,26 @@ struct BatchDev {
     int* error;                // device error bits
     int scatter_rara;          // deliver over the static RA->RA lists (test trial)
     int* soma_bits;            // [B][n_ra] soma-spike step bits of the interval (growth), or null
-    // Group growth: rows that have deliveries to make in an interval (rows that
-    // spiked in it, and rows whose earlier spikes still have events pending).
-    int2* act_rows;            // [2][act_cap] (member, row) lists by interval parity, or null
-    int* act_cnt;              // [2]
+    // Group growth: the rows that have deliveries to make in an interval --
+    // rows that spiked in it and rows whose earlier spikes have streams open.
+    // Two queues (warp path, heavy block path), each by interval parity.
+    int2* act_rows;            // [2 paths][2 parities][act_cap] (member, row), or null
+    int* act_cnt;              // [2 paths][2 parities]
     int act_cap;
     int member;                // index of this batch in its group
-    int* row_stamp;            // [B][n_ra] 1 + the last interval the row was queued for
+    const int* live_streams;   // [B][n_ra] open delivery streams of each row (the growth state)
+    int heavy;                 // the rows take the heavy (block) path
 };
 
-// Queues row x of a group growth member for interval q (once per interval).
+// Queues row x of a group growth member for interval q if it has deliveries to make.
 template <class R>
-__device__ __forceinline__ void queue_row(const BatchDev<R>& bt, int q, int x)
+__device__ __forceinline__ void queue_row(const BatchDev<R>& bt, int q, int x, uint32_t soma)
 {
-    const int tag = q + 1;
-    if (atomicMax(&bt.row_stamp[x], tag) < tag) {
-        const int pos = atomicAdd(&bt.act_cnt[q & 1], 1);
-        if (pos < bt.act_cap) bt.act_rows[(size_t)(q & 1) * bt.act_cap + pos] = make_int2(bt.member, x);
-        else atomicOr(bt.error, kErrEventCapacity);
-    }
+    if (!soma && bt.live_streams[x] == 0) return;
+    const int list = (bt.heavy ? 2 : 0) + (q & 1);
+    const int pos = atomicAdd(&bt.act_cnt[list], 1);
+    if (pos < bt.act_cap) bt.act_rows[(size_t)list * bt.act_cap + pos] = make_int2(bt.member, x);
+    else atomicOr(bt.error, kErrEventCapacity);
 }
 
 // First step s' >= s with T[s'] >= T[s] + d, or num_steps if the trial ends first.
@@ -376,7 +377,7 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
             }
         }
         if (bt.soma_bits) bt.soma_bits[x] = (int)soma;
-        if (soma && bt.act_rows) queue_row(bt, q, (int)x);
+        if (bt.act_rows) queue_row(bt, q, (int)x, soma);
     }
     scatter_warp(soma, i, s0, n.T, n.num_steps, n.syncidx, n.ring, n.ra2i_off, n.ra2i_tgt, n.ra2i_wq, n.ra2i_d,
                  bt.ring_i_exc, (size_t)bt.B * n.n_i, (size_t)b * n.n_i);
@@ -488,7 +489,7 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
                 record_spikes(bt.spk_count, bt.spk_buf, bt.spk_cap, bt.error, b, i, kSpikeDend, de, s0);
             }
             if (bt.soma_bits && (k == 0 || v1)) bt.soma_bits[x] = (int)so;
-            if (so && bt.act_rows) queue_row(bt, q, (int)x);
+            if (bt.act_rows && (k == 0 || v1)) queue_row(bt, q, (int)x, so);
         }
     }
     for (int k = 0; k < 2; ++k) {
