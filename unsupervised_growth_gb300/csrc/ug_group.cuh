@@ -14,9 +14,9 @@
 //
 // Growth rows: a row has deliveries to make in an interval only if it spiked
 // in the interval or an earlier spike's stream is still open.  The RA kernel
-// queues spiking rows and the row kernel re-queues rows whose streams stay
-// open, so the row kernel visits exactly the rows with work, across all
-// members, one warp per row.
+// queues exactly those rows, so the row kernels visit only rows with work,
+// across all members: one warp per row, or one block per row for networks of
+// kHeavyMinRows neurons or more.
 #pragma once
 #include "ug_growth.cuh"
 
@@ -41,7 +41,8 @@ __device__ __forceinline__ void copy_words(T& dst, const T& src, int tid, int nt
     for (int k = tid; k < (int)(sizeof(T) / 4); k += nthreads) d[k] = s[k];
 }
 
-// Walks this block's items; f(member, bx, by) runs with the member staged in M.
+// Walks this block's items (grid-stride); f(member, bx, by) runs with the
+// member staged in M.
 template <class R, class F>
 __device__ __forceinline__ void for_items(const GroupMember<R>* members, const int4* items, int count,
                                           GroupMember<R>& M, F&& f)
@@ -144,7 +145,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) kl_growth_rows(const GroupMemb
         }
         const GroupMember<R>& m = M[w];
         const int b = it.y / m.n.n_ra, i = it.y - b * m.n.n_ra;
-        g_row(m.g, m.n, m.bt, b, i, s0, s1, sh_T, sh, lane);
+        g_row(m.g, m.n, m.bt, soma_slice(m.bt, m.n, q), b, i, s0, s1, sh_T, sh, lane);
         __syncwarp();
     }
 }
@@ -176,18 +177,19 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) kl_growth_rows_heavy(const G
             cur = it.x;
         }
         const int b = it.y / M.n.n_ra, i = it.y - b * M.n.n_ra;
-        g_row_heavy(M.g, M.n, M.bt, b, i, s0, s1, sh_T, sh, hs);
+        g_row_heavy(M.g, M.n, M.bt, soma_slice(M.bt, M.n, q), b, i, s0, s1, sh_T, sh, hs);
     }
 }
 
 // items: (member, 0, b)
 template <class R>
 __global__ void __launch_bounds__(1024) kl_growth_newpost(const GroupMember<R>* members, const int4* items,
-                                                          const int* count, int s0, int s1)
+                                                          const int* count, int q, int s0, int s1)
 {
     __shared__ GroupMember<R> M;
-    for_items(members, items, *count, M,
-              [&](const GroupMember<R>& m, int, int b) { g_newpost_body(m.g, m.n, m.bt, b, s0, s1); });
+    for_items(members, items, *count, M, [&](const GroupMember<R>& m, int, int b) {
+        g_newpost_body(m.g, m.n, soma_slice(m.bt, m.n, q), b, s0, s1);
+    });
 }
 
 template <class R>

@@ -59,6 +59,8 @@ struct GrowthDev {
     int* post_step;         // [B][n][kPostRing] sync steps of post events, ring
     int* post_cnt;          // [B][n]
     double* post_last;      // [B][n] time of the newest post event (-1e300: none this trial)
+    double* spike_last;     // [B][n] time of the row's newest somatic spike (-1e300: none this trial)
+    double max_delay;       // bound on every RA->RA delay the network can have
     int* st_step;           // [B][n][kMaxStreams] spike step of each live stream
     int* st_cursor;         // [B][n][kMaxStreams]
     int* st_len;            // [B][n][kMaxStreams] targets in the stream (n-1, or the snapshot size)
@@ -218,6 +220,7 @@ __device__ __forceinline__ int g_open_stream(const GrowthDev& g, size_t r, int s
     }
     const int slot = (head + num) % kMaxStreams;
     stS[slot] = s;
+    g.spike_last[r] = Ts;
     stC[slot] = 0;
     const int sc = g.sup_cnt[r];
     if (sc == g.sp.Nss) {
@@ -567,12 +570,13 @@ __device__ __forceinline__ void g_process(const GrowthDev& g, const NetDev<R>& n
 // (sh_T holds T[s0..s1]); a spike at `from` has already opened its stream
 // when opened_at_from is set.  head / num: the row's stream ring.
 template <class R>
-__device__ __forceinline__ void g_row_range(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b,
-                                            int i, int s0, int from, int to, bool opened_at_from,
-                                            const double* sh_T, RowShared& sh, int lane, int& head, int& num)
+__device__ __forceinline__ void g_row_range(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt,
+                                            const int* soma, int b, int i, int s0, int from, int to,
+                                            bool opened_at_from, const double* sh_T, RowShared& sh, int lane,
+                                            int& head, int& num)
 {
     const size_t r = (size_t)b * g.n + i;
-    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    const uint32_t bits = (uint32_t)soma[(size_t)b * n.n_ra + i];
     const int s1 = to;
     int* stS = g.st_step + r * kMaxStreams;
     int* stC = g.st_cursor + r * kMaxStreams;
@@ -670,14 +674,14 @@ __device__ __forceinline__ void g_row_range(const GrowthDev& g, const NetDev<R>&
 // One warp, row i of instance b over the whole interval s0..s1.  Returns the
 // row's live streams after it.
 template <class R>
-__device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int i,
-                                     int s0, int s1, const double* sh_T, RowShared& sh, int lane)
+__device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, const int* soma,
+                                     int b, int i, int s0, int s1, const double* sh_T, RowShared& sh, int lane)
 {
     const size_t r = (size_t)b * g.n + i;
-    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    const uint32_t bits = (uint32_t)soma[(size_t)b * n.n_ra + i];
     int head = g.st_head[r], num = g.st_num[r];
     if (bits == 0 && num == 0) return 0;
-    g_row_range(g, n, bt, b, i, s0, s0, s1, false, sh_T, sh, lane, head, num);
+    g_row_range(g, n, bt, soma, b, i, s0, s0, s1, false, sh_T, sh, lane, head, num);
     if (lane == 0) {
         g.st_head[r] = head;
         g.st_num[r] = num;
@@ -710,13 +714,13 @@ struct HeavyShared {
 
 // Block: queued row i of instance b in the interval s0..s1 (sh_T = T[s0..s1]).
 template <class R>
-__device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b,
-                                            int i, int s0, int s1, const double* sh_T, RowShared& sh,
-                                            HeavyShared& hs)
+__device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt,
+                                            const int* soma, int b, int i, int s0, int s1, const double* sh_T,
+                                            RowShared& sh, HeavyShared& hs)
 {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const size_t r = (size_t)b * g.n + i;
-    const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
+    const uint32_t bits = (uint32_t)soma[(size_t)b * n.n_ra + i];
     const int from = bits ? s0 + __ffs(bits) - 1 : s0;   // the spike, or the interval's start
     int* stS = g.st_step + r * kMaxStreams;
     int* stC = g.st_cursor + r * kMaxStreams;
@@ -729,7 +733,8 @@ __device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>&
         int head = g.st_head[r], num = g.st_num[r];
         int mode = 1;
         if (bits) {
-            if (from > s0 && num > 0) g_row_range(g, n, bt, b, i, s0, s0, from - 1, false, sh_T, sh, lane, head, num);
+            if (from > s0 && num > 0)
+                g_row_range(g, n, bt, soma, b, i, s0, s0, from - 1, false, sh_T, sh, lane, head, num);
             if (lane == 0) {
                 const int before = num;
                 num = g_open_stream(g, r, from, sh_T[from - s0], Drow, head, num, stS, stC, stL, stT);
@@ -849,7 +854,7 @@ __device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>&
     __syncthreads();
     if (w == 0) {
         int head = hs.head, num = hs.num;
-        g_row_range(g, n, bt, b, i, s0, from, s1, bits != 0, sh_T, sh, lane, head, num);
+        g_row_range(g, n, bt, soma, b, i, s0, from, s1, bits != 0, sh_T, sh, lane, head, num);
         if (lane == 0) {
             g.st_head[r] = head;
             g.st_num[r] = num;
@@ -858,8 +863,16 @@ __device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>&
     __syncthreads();
 }
 
+// The interval's somatic spike bits of each RA neuron, by interval parity (the
+// growth kernels of interval q read them while the integrator of q + 1 runs).
 template <class R>
-__global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0,
+__device__ __forceinline__ const int* soma_slice(const BatchDev<R>& bt, const NetDev<R>& n, int q)
+{
+    return bt.soma_bits + (size_t)(q & 1) * bt.B * n.n_ra;
+}
+
+template <class R>
+__global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int q, int s0,
                                                                 int s1)
 {
     extern __shared__ __align__(16) unsigned char row_smem[];
@@ -874,83 +887,74 @@ __global__ void __launch_bounds__(32 * kRowWarps) k_growth_rows(GrowthDev g, Net
         if (lane == 0) atomicOr(g.error, kErrEventCapacity);
         return;
     }
-    g_row(g, n, bt, b, i, s0, s1, sh_T, reinterpret_cast<RowShared*>(row_smem)[w], lane);
+    g_row(g, n, bt, soma_slice(bt, n, q), b, i, s0, s1, sh_T, reinterpret_cast<RowShared*>(row_smem)[w], lane);
 }
 
 // New post-synaptic events of the interval in the reference's order: steps
-// ascending, neurons ascending within a step (:8952-8967), judged against the
-// post events recorded before this interval; then the sync time is appended
-// to each (:9385-9386).  One block per instance.
+// ascending, neurons ascending within a step (:8952-8967), each judged against
+// the post events recorded before this interval (the newest: post_last); then
+// the sync time is appended once per entry (:9385-9386).  One block per
+// instance: each thread finds its neurons' entries and appends their post
+// events (every entry of a neuron appends the same sync time, so their order
+// does not matter), and the block sorts the entries by (step, neuron).
+constexpr int kNewpostCap = 4096;   // entries per interval and instance
+
 template <class R>
-__device__ __forceinline__ void g_newpost_body(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& bt, int b, int s0,
-                                               int s1)
+__device__ __forceinline__ void g_newpost_body(const GrowthDev& g, const NetDev<R>& n, const int* soma, int b,
+                                               int s0, int s1)
 {
     __shared__ int cnt;
-    __shared__ int wsum[32];
-    // most intervals hold no somatic spike at all
-    int any = 0;
-    for (int i = threadIdx.x; i < g.n; i += blockDim.x) any |= bt.soma_bits[(size_t)b * n.n_ra + i];
-    if (!__syncthreads_or(any)) {
-        if (threadIdx.x == 0) g.newpost_cnt[b] = 0;
-        return;
-    }
+    __shared__ unsigned keys[kNewpostCap];   // step offset << 27 | neuron
     if (threadIdx.x == 0) cnt = 0;
     __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int s = s0; s <= s1; ++s) {
-        const double Ts = n.T[s];
-        for (int base = 0; base < g.n; base += blockDim.x) {
-            const int i = base + threadIdx.x;
-            int flag = 0;
-            if (i < g.n) {
-                const uint32_t bits = (uint32_t)bt.soma_bits[(size_t)b * n.n_ra + i];
-                if ((bits >> (s - s0)) & 1u) {
-                    const int np = post_num(g, b, i);
-                    if (np == 0) flag = 1;
-                    else if (Ts > n.T[post_at(g, b, i, np - 1)] + 30.0) flag = 1;
-                }
-            }
-            // block-wide ordered compaction
-            const unsigned m = __ballot_sync(0xffffffffu, flag);
-            if (lane == 0) wsum[warp] = __popc(m);
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                int acc = cnt;
-                for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-                    const int c = wsum[w];
-                    wsum[w] = acc;
-                    acc += c;
-                }
-                cnt = acc;
-            }
-            __syncthreads();
-            if (flag) {
-                const int pos = wsum[warp] + __popc(m & ((1u << lane) - 1u));
-                if (pos < g.n * 16) g.newpost[(size_t)b * g.n * 16 + pos] = i;
-                else atomicOr(g.error, kErrPostCapacity);
-            }
-            __syncthreads();
+    const double Tsync = n.T[s1];
+    for (int i = threadIdx.x; i < g.n; i += blockDim.x) {
+        const uint32_t bits = (uint32_t)soma[(size_t)b * n.n_ra + i];
+        if (!bits) continue;
+        const size_t ri = (size_t)b * g.n + i;
+        const double pl = g.post_last[ri];   // -1e300 when the neuron has no post event yet
+        uint32_t mask = 0;
+        for (uint32_t m = bits; m; m &= m - 1) {
+            const int k = __ffs(m) - 1;
+            if (n.T[s0 + k] > pl + 30.0) mask |= 1u << k;
         }
+        if (!mask) continue;
+        const int c = __popc(mask);
+        int pos = atomicAdd(&cnt, c);
+        for (uint32_t m = mask; m; m &= m - 1) {
+            if (pos < kNewpostCap) keys[pos] = ((unsigned)(__ffs(m) - 1) << 27) | (unsigned)i;
+            ++pos;
+        }
+        for (int e = 0; e < c; ++e) {
+            g.post_step[ri * kPostRing + (g.post_cnt[ri] % kPostRing)] = s1;
+            g.post_cnt[ri] += 1;
+        }
+        g.post_last[ri] = Tsync;
     }
     __syncthreads();
-    const int total = cnt < g.n * 16 ? cnt : g.n * 16;
-    if (threadIdx.x == 0) g.newpost_cnt[b] = total;
-    // append the sync time; a neuron listed twice gets two entries, in list order
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < total; ++k) {
-            const int j = g.newpost[(size_t)b * g.n * 16 + k];
-            const size_t rj = (size_t)b * g.n + j;
-            g.post_step[rj * kPostRing + (g.post_cnt[rj] % kPostRing)] = s1;
-            g.post_cnt[rj] += 1;
-            g.post_last[rj] = n.T[s1];
+    const int K = cnt;
+    if (K > kNewpostCap || K > g.n * 16) {
+        if (threadIdx.x == 0) {
+            atomicOr(g.error, kErrPostCapacity);
+            g.newpost_cnt[b] = 0;
         }
+        return;
     }
+    // rank sort (the keys are distinct)
+    for (int e = threadIdx.x; e < K; e += blockDim.x) {
+        const unsigned key = keys[e];
+        int rank = 0;
+        for (int j = 0; j < K; ++j) rank += keys[j] < key;
+        g.newpost[(size_t)b * g.n * 16 + rank] = (int)(key & ((1u << 27) - 1u));
+    }
+    if (threadIdx.x == 0) g.newpost_cnt[b] = K;
 }
 
 template <class R>
-__global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int s0, int s1)
+__global__ void __launch_bounds__(1024) k_growth_newpost(GrowthDev g, NetDev<R> n, BatchDev<R> bt, int q, int s0,
+                                                         int s1)
 {
-    g_newpost_body(g, n, bt, (int)blockIdx.x, s0, s1);
+    g_newpost_body(g, n, soma_slice(bt, n, q), (int)blockIdx.x, s0, s1);
 }
 
 // LTP / LTD of every row against the interval's new post events, then axon
@@ -967,7 +971,10 @@ __device__ __forceinline__ void g_ltp_body(const GrowthDev& g, const NetDev<R>& 
     const double now = n.T[s1];
     const bool saturated = g.sup_cnt[r] == sp.Nss;
     const int* list = g.newpost + (size_t)b * g.n * 16;
-    for (int k = 0; k < total; ++k) {
+    // a pre event of row i arrives at most max_delay after the row's last spike:
+    // a row silent for longer than the window plus that has none inside it
+    const int kmax = g.spike_last[r] + g.max_delay >= now - 100.0 ? total : 0;
+    for (int k = 0; k < kmax; ++k) {
         const int post = list[k];
         if (post == i) continue;
         if (saturated) {
@@ -1034,6 +1041,7 @@ __device__ __forceinline__ void g_reset_body(const GrowthDev& g, int part, int n
     for (size_t k = tid; k < nr; k += (size_t)nparts * blockDim.x) {
         g.post_cnt[k] = 0;
         g.post_last[k] = -1e300;
+        g.spike_last[k] = -1e300;
         g.st_head[k] = 0;
         g.st_num[k] = 0;
     }

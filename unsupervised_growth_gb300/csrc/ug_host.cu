@@ -275,12 +275,13 @@ private:
     bool rara_dirty_ = false;       // device synapse lists changed since the static lists were built
     ug::GrowthDev gd_{};
     DevMem gW_, gD_, gPerm_, gActive_, gSuper_, gActList_, gActCnt_, gSupList_, gSupCnt_, gRemod_, gPreStep_,
-        gPreCnt_, gPostStep_, gPostCnt_, gPostLast_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
+        gPreCnt_, gPostStep_, gPostCnt_, gPostLast_, gSpikeLast_, gStStep_, gStCur_, gStLen_, gStTgt_, gStHead_, gStNum_, gNewpost_,
         gNewpostCnt_, gSomaBits_, gBad_, gRep_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
     std::vector<int> syncidx_;
     std::vector<double> ra_decay_, i_decay_;
+    double max_delay_ = 0.0;   // bound on every delay, including those a replaced neuron can get
 };
 
 template <class R>
@@ -424,6 +425,7 @@ ug_status NetImpl<R>::init_host(const ug_network_desc* d, int spike_cap_per_neur
                                             std::fabs(H.conn.delay_constant));
     if (!(max_delay >= 0.0) || max_delay > 1000.0) return fail(UG_EINVAL, "axonal delays must lie in [0, 1000] ms");
     ring = (int)std::floor(max_delay / 0.24) + 4;
+    max_delay_ = max_delay;
     return UG_OK;
 }
 
@@ -615,7 +617,7 @@ size_t NetImpl<R>::device_bytes() const
                             &mean_inj_})
         t += m->bytes();
     for (const DevMem* m : {&gW_, &gD_, &gPerm_, &gActive_, &gSuper_, &gActList_, &gActCnt_, &gSupList_, &gSupCnt_,
-                            &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gPostLast_, &gStStep_, &gStCur_, &gStLen_,
+                            &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gPostLast_, &gSpikeLast_, &gStStep_, &gStCur_, &gStLen_,
                             &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_})
         t += m->bytes();
     return t;
@@ -638,8 +640,8 @@ size_t NetImpl<R>::footprint(int kind, int B) const
     t += (size_t)ring * 8 * (2 * bra + bi) + (size_t)B * (cap * 8 + 16);
     if (kind == 1) {
         const size_t nn = nra * nra;
-        t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 8 + 3 * 4 * ug::kMaxStreams +
-                              4 * ug::kMaxStreams * ug::kMaxNss + 8 + 64 + 4 + 4 + 4) + 8;
+        t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 16 + 3 * 4 * ug::kMaxStreams +
+                              4 * ug::kMaxStreams * ug::kMaxNss + 8 + 64 + 8 + 4 + 4) + 8;
     }
     return t;
 }
@@ -788,6 +790,8 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     UG_TRY(gPostStep_.alloc((size_t)n * ug::kPostRing * sizeof(int)));
     UG_TRY(gPostCnt_.alloc((size_t)n * sizeof(int)));
     UG_TRY(gPostLast_.alloc((size_t)n * sizeof(double)));
+    UG_TRY(gSpikeLast_.alloc((size_t)n * sizeof(double)));
+    if (n >= (1 << 27)) return fail(UG_EINVAL, "growth networks are limited to 2^27 HVC(RA) neurons");
     UG_TRY(gStStep_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
     UG_TRY(gStCur_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
     UG_TRY(gStLen_.alloc((size_t)n * ug::kMaxStreams * sizeof(int)));
@@ -796,7 +800,7 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     UG_TRY(gStNum_.alloc((size_t)n * sizeof(int)));
     UG_TRY(gNewpost_.alloc((size_t)n * 16 * sizeof(int)));
     UG_TRY(gNewpostCnt_.alloc(sizeof(int)));
-    UG_TRY(gSomaBits_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gSomaBits_.alloc(2 * (size_t)n * sizeof(int)));
     UG_TRY(gBad_.alloc(sizeof(int)));
     UG_TRY(gRep_.alloc((size_t)n * sizeof(int)));
     ug::GrowthDev& g = gd_;
@@ -813,6 +817,8 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     g.sup_list = gSupList_.as<int>(); g.sup_cnt = gSupCnt_.as<int>(); g.remodeled = gRemod_.as<int>();
     g.pre_step = gPreStep_.as<short>(); g.pre_cnt = gPreCnt_.as<uint8_t>();
     g.post_step = gPostStep_.as<int>(); g.post_cnt = gPostCnt_.as<int>(); g.post_last = gPostLast_.as<double>();
+    g.spike_last = gSpikeLast_.as<double>();
+    g.max_delay = max_delay_;
     g.st_step = gStStep_.as<int>(); g.st_cursor = gStCur_.as<int>(); g.st_len = gStLen_.as<int>();
     g.st_tgt = gStTgt_.as<int>(); g.st_head = gStHead_.as<int>(); g.st_num = gStNum_.as<int>();
     g.newpost = gNewpost_.as<int>(); g.newpost_cnt = gNewpostCnt_.as<int>();
@@ -830,13 +836,15 @@ ug_status NetImpl<R>::issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launc
     UG_CUDA(ug::launch_growth_reset<R>(gd_, lc));
     ++cnt;
     const int Q = (int)sync_steps.size();
+    bool tail_open = false;
     for (int q = 0; q < Q; ++q) {
         const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
         UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, lc));
-        UG_CUDA(ug::launch_growth_sync<R>(gd_, nd_, bd_, s0, sync_steps[q], lc));
+        UG_CUDA(ug::launch_growth_sync<R>(gd_, nd_, bd_, q, s0, sync_steps[q], lc, tail_open));
         cnt += 5;
     }
     UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
+    UG_CUDA(ug::launch_tail_join(lc, tail_open));
     UG_CUDA(ug::launch_growth_epilogue<R>(gd_, lc));
     cnt += 3;
     if (launches) *launches += cnt;
@@ -1407,6 +1415,8 @@ struct ug_ctx {
     cudaStream_t stream = nullptr;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t tail = nullptr;
+    cudaEvent_t tail_fork = nullptr, tail_join = nullptr;
     ug::KernelTimer timer;
     ug::LaunchCtx launch_ctx()
     {
@@ -1415,6 +1425,9 @@ struct ug_ctx {
         lc.side = side;
         lc.fork = fork;
         lc.join = join;
+        lc.tail = tail;
+        lc.tail_fork = tail_fork;
+        lc.tail_join = tail_join;
         lc.timer = timer.enabled ? &timer : nullptr;
         return lc;
     }
@@ -1769,6 +1782,9 @@ ug_status ug_create(ug_ctx** out, const ug_runtime_opts* opts)
     UG_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
     UG_CUDA(cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming));
     UG_CUDA(cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming));
+    UG_CUDA(cudaStreamCreateWithFlags(&c->tail, cudaStreamNonBlocking));
+    UG_CUDA(cudaEventCreateWithFlags(&c->tail_fork, cudaEventDisableTiming));
+    UG_CUDA(cudaEventCreateWithFlags(&c->tail_join, cudaEventDisableTiming));
     c->stream = c->own;
     *out = c.release();
     return UG_OK;
@@ -1785,6 +1801,10 @@ void ug_destroy(ug_ctx* ctx)
     ctx->group.reset();
     ctx->nets.clear();
     ctx->timer.clear(true);
+    if (ctx->tail) cudaStreamSynchronize(ctx->tail);
+    if (ctx->tail_fork) cudaEventDestroy(ctx->tail_fork);
+    if (ctx->tail_join) cudaEventDestroy(ctx->tail_join);
+    if (ctx->tail) cudaStreamDestroy(ctx->tail);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->join) cudaEventDestroy(ctx->join);
     if (ctx->side) cudaStreamDestroy(ctx->side);

@@ -6,8 +6,8 @@ template cudaError_t launch_trial_init<float>(const NetDev<float>&, const BatchD
 template cudaError_t launch_interval<float>(const NetDev<float>&, const BatchDev<float>&, int, int, int,
                                             const RAStep<float>&, const IStep<float>&, const LaunchCtx&);
 template cudaError_t launch_growth_reset<float>(const GrowthDev&, const LaunchCtx&);
-template cudaError_t launch_growth_sync<float>(const GrowthDev&, const NetDev<float>&, const BatchDev<float>&, int, int,
-                                             const LaunchCtx&);
+template cudaError_t launch_growth_sync<float>(const GrowthDev&, const NetDev<float>&, const BatchDev<float>&, int, int, int,
+                                             const LaunchCtx&, bool&);
 template cudaError_t launch_growth_epilogue<float>(const GrowthDev&, const LaunchCtx&);
 template cudaError_t launch_growth_remove<float>(const GrowthDev&, const int*, int, cudaStream_t);
 template cudaError_t launch_check_bad<float>(const NetDev<float>&, const BatchDev<float>&, int*, cudaStream_t);

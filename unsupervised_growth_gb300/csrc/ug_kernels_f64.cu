@@ -6,8 +6,8 @@ template cudaError_t launch_trial_init<double>(const NetDev<double>&, const Batc
 template cudaError_t launch_interval<double>(const NetDev<double>&, const BatchDev<double>&, int, int, int,
                                              const RAStep<double>&, const IStep<double>&, const LaunchCtx&);
 template cudaError_t launch_growth_reset<double>(const GrowthDev&, const LaunchCtx&);
-template cudaError_t launch_growth_sync<double>(const GrowthDev&, const NetDev<double>&, const BatchDev<double>&, int, int,
-                                             const LaunchCtx&);
+template cudaError_t launch_growth_sync<double>(const GrowthDev&, const NetDev<double>&, const BatchDev<double>&, int, int, int,
+                                             const LaunchCtx&, bool&);
 template cudaError_t launch_growth_epilogue<double>(const GrowthDev&, const LaunchCtx&);
 template cudaError_t launch_growth_remove<double>(const GrowthDev&, const int*, int, cudaStream_t);
 template cudaError_t launch_check_bad<double>(const NetDev<double>&, const BatchDev<double>&, int*, cudaStream_t);

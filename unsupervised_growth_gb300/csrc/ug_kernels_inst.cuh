@@ -103,18 +103,39 @@ cudaError_t launch_growth_reset(const GrowthDev& g, const LaunchCtx& lc)
     return cudaGetLastError();
 }
 
-// Deliveries of the interval's RA spikes to RA targets, then the sync's post
-// events, LTP and axon remodeling.
-template <class R>
-cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int s0, int s1,
-                               const LaunchCtx& lc)
+// The tail of an interval goes on lc.tail when there is one (and no timer).
+inline cudaError_t tail_fork(const LaunchCtx& lc, cudaStream_t* ts)
 {
+    *ts = lc.main;
+    if (lc.timer || !lc.tail || lc.tail == lc.main) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(lc.tail_fork, lc.main);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.tail, lc.tail_fork, 0);
+    *ts = lc.tail;
+    return e;
+}
+
+// Deliveries of the interval's RA spikes to RA targets (after the previous
+// interval's tail), then the sync's post events, LTP and axon remodeling as
+// this interval's tail.
+template <class R>
+cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1,
+                               const LaunchCtx& lc, bool& tail_open)
+{
+    cudaError_t e = launch_tail_join(lc, tail_open);
+    if (e != cudaSuccess) return e;
     const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
     const dim3 wrows((g.n + kRowWarps - 1) / kRowWarps, g.B);
-    UG_TIMED(lc, "k_growth_rows", (k_growth_rows<R><<<wrows, 32 * kRowWarps, kRowWarps * sizeof(RowShared), lc.main>>>(g, n, b, s0, s1)));
-    UG_TIMED(lc, "k_growth_newpost", (k_growth_newpost<R><<<g.B, 1024, 0, lc.main>>>(g, n, b, s0, s1)));
-    UG_TIMED(lc, "k_growth_ltp", (k_growth_ltp<R><<<rows, kBlock, 0, lc.main>>>(g, n, s1)));
-    return cudaGetLastError();
+    UG_TIMED(lc, "k_growth_rows", (k_growth_rows<R><<<wrows, 32 * kRowWarps, kRowWarps * sizeof(RowShared), lc.main>>>(g, n, b, q, s0, s1)));
+    cudaStream_t ts;
+    e = tail_fork(lc, &ts);
+    if (e != cudaSuccess) return e;
+    UG_TIMED(lc, "k_growth_newpost", (k_growth_newpost<R><<<g.B, 1024, 0, ts>>>(g, n, b, q, s0, s1)));
+    UG_TIMED(lc, "k_growth_ltp", (k_growth_ltp<R><<<rows, kBlock, 0, ts>>>(g, n, s1)));
+    if (ts != lc.main) {
+        e = cudaEventRecord(lc.tail_join, ts);
+        tail_open = true;
+    }
+    return e == cudaSuccess ? cudaGetLastError() : e;
 }
 
 template <class R>
@@ -199,6 +220,7 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
         ++cnt;
     }
     const bool fork = d.fork && !lc.timer && lc.side && lc.side != lc.main;
+    bool tail_open = false;
     const int Q = (int)sync_steps.size();
     for (int q = 0; q <= Q; ++q) {
         const int s0 = q == 0 ? 1 : (q < Q ? sync_steps[q - 1] + 1 : num_steps);
@@ -219,6 +241,8 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
             if (e != cudaSuccess) return e;
         }
         if (growth && q < Q) {
+            e = launch_tail_join(lc, tail_open);
+            if (e != cudaSuccess) return e;
             // heavy rows (a block each) beside the warp-path rows: different rows, disjoint state
             const bool rfork = !lc.timer && lc.side && lc.side != lc.main;
             if (rfork) {
@@ -233,11 +257,21 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
                 if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.main, lc.join, 0);
                 if (e != cudaSuccess) return e;
             }
-            UG_TIMED(lc, "k_growth_newpost", (kl_growth_newpost<R><<<d.grid[kListNewpost], 1024, 0, lc.main>>>(mem, d.items[kListNewpost], c + kListNewpost, s0, s1)));
-            UG_TIMED(lc, "k_growth_ltp", (kl_growth_ltp<R><<<d.grid[kListLtp], kBlock, 0, lc.main>>>(mem, d.items[kListLtp], c + kListLtp, s1)));
+            cudaStream_t ts;
+            e = tail_fork(lc, &ts);
+            if (e != cudaSuccess) return e;
+            UG_TIMED(lc, "k_growth_newpost", (kl_growth_newpost<R><<<d.grid[kListNewpost], 1024, 0, ts>>>(mem, d.items[kListNewpost], c + kListNewpost, q, s0, s1)));
+            UG_TIMED(lc, "k_growth_ltp", (kl_growth_ltp<R><<<d.grid[kListLtp], kBlock, 0, ts>>>(mem, d.items[kListLtp], c + kListLtp, s1)));
+            if (ts != lc.main) {
+                e = cudaEventRecord(lc.tail_join, ts);
+                if (e != cudaSuccess) return e;
+                tail_open = true;
+            }
             cnt += 4;
         }
     }
+    e = launch_tail_join(lc, tail_open);
+    if (e != cudaSuccess) return e;
     if (growth) {
         UG_TIMED(lc, "k_growth_epilogue", (kl_growth_epilogue<R><<<d.grid[kListLtp], kBlock, 0, lc.main>>>(mem, d.items[kListLtp], c + kListLtp)));
         ++cnt;

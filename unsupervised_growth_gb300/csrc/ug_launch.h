@@ -91,6 +91,10 @@ struct LaunchCtx {
     cudaStream_t main = nullptr;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
+    // growth: the STDP tail of interval q (new post events, LTP) runs here,
+    // beside the integrators of interval q + 1
+    cudaStream_t tail = nullptr;
+    cudaEvent_t tail_fork = nullptr, tail_join = nullptr;
     KernelTimer* timer = nullptr;
 };
 
@@ -104,9 +108,18 @@ cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int
 // Growth trial pieces (ug_growth.cuh).
 template <class R>
 cudaError_t launch_growth_reset(const GrowthDev& g, const LaunchCtx& lc);
+// tail_open: the previous interval's STDP tail is still running on lc.tail;
+// launch_growth_sync waits for it before the deliveries and leaves its own open.
 template <class R>
-cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int s0, int s1,
-                               const LaunchCtx& lc);
+cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1,
+                               const LaunchCtx& lc, bool& tail_open);
+// Joins an open tail back into lc.main.
+inline cudaError_t launch_tail_join(const LaunchCtx& lc, bool& tail_open)
+{
+    if (!tail_open) return cudaSuccess;
+    tail_open = false;
+    return cudaStreamWaitEvent(lc.main, lc.tail_join, 0);
+}
 template <class R>
 cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc);
 template <class R>

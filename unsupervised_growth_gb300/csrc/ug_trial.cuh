@@ -84,7 +84,7 @@ struct BatchDev {
     int spk_cap;
     int* error;                // device error bits
     int scatter_rara;          // deliver over the static RA->RA lists (test trial)
-    int* soma_bits;            // [B][n_ra] soma-spike step bits of the interval (growth), or null
+    int* soma_bits;            // [2][B][n_ra] soma-spike step bits of the interval by its parity (growth), or null
     // Group growth: the rows that have deliveries to make in an interval --
     // rows that spiked in it and rows whose earlier spikes have streams open.
     // Two queues (warp path, heavy block path), each by interval parity.
@@ -376,7 +376,7 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
                 record_spikes(bt.spk_count, bt.spk_buf, bt.spk_cap, bt.error, b, i, kSpikeDend, dend, s0);
             }
         }
-        if (bt.soma_bits) bt.soma_bits[x] = (int)soma;
+        if (bt.soma_bits) bt.soma_bits[(size_t)(q & 1) * bt.B * n.n_ra + x] = (int)soma;
         if (bt.act_rows) queue_row(bt, q, (int)x, soma);
     }
     scatter_warp(soma, i, s0, n.T, n.num_steps, n.syncidx, n.ring, n.ra2i_off, n.ra2i_tgt, n.ra2i_wq, n.ra2i_d,
@@ -488,7 +488,7 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
                 if (bt.ra_first_dend[x] < 0) bt.ra_first_dend[x] = s0 + __ffs(de) - 1;
                 record_spikes(bt.spk_count, bt.spk_buf, bt.spk_cap, bt.error, b, i, kSpikeDend, de, s0);
             }
-            if (bt.soma_bits && (k == 0 || v1)) bt.soma_bits[x] = (int)so;
+            if (bt.soma_bits && (k == 0 || v1)) bt.soma_bits[(size_t)(q & 1) * bt.B * n.n_ra + x] = (int)so;
             if (bt.act_rows && (k == 0 || v1)) queue_row(bt, q, (int)x, so);
         }
     }
