@@ -158,6 +158,22 @@ def _fp64_plain(net, device, trial, rn32):
     return fp64_s, acc
 
 
+TRIALS_PER_RANK = 1_000_000   # rank r draws the noise streams of trials [r * 1e6, (r + 1) * 1e6)
+
+
+def replica_first_trial(rank: int) -> int:
+    """First trial index of a replica: replicas never share a noise stream."""
+    return rank * TRIALS_PER_RANK
+
+
+def max_over_ranks(x: float, dist, device) -> float:
+    """The slowest replica's time (the job finishes with it)."""
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -182,7 +198,9 @@ def run_ours(args, rank, world, local_rank):
     eng.set_stream(stream.cuda_stream)
     rn = eng.load_network(net)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    first = rank * 1_000_000
+    first = replica_first_trial(rank)
+    if (args.warmup + 2 * args.steps + 1) * BATCH > TRIALS_PER_RANK:
+        raise SystemExit("too many trials per replica for its range of noise streams")
 
     for w in range(args.warmup):
         rn.run_test_trials(first + w * BATCH, BATCH)
@@ -207,9 +225,7 @@ def run_ours(args, rank, world, local_rank):
     launches = eng.launch_count() - launches0
     total_ms = sum(step_ms)
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(total_ms, dist, "cuda")
         dist.barrier()
 
     # e2e through the C ABI: trial list H2D, batch, per-neuron spike statistics D2H

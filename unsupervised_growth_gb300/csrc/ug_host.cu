@@ -656,6 +656,8 @@ ug_status NetImpl<R>::prepare_test(uint32_t first_trial, int n_trials, cudaStrea
     bd_.B = n_trials;
     bd_.kick_on = 1;
     bd_.scatter_rara = 1;
+    // capacity errors belong to the batch that raised them
+    UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
     B_ = n_trials;
     std::vector<uint32_t> tr(n_trials);
     std::vector<double> mi(n_trials, kMeanInjectionTest);
@@ -910,6 +912,7 @@ ug_status NetImpl<R>::prepare_growth(uint32_t trial, int training, cudaStream_t 
     bd_.scatter_rara = 0;
     bd_.soma_bits = gSomaBits_.as<int>();
     B_ = 1;
+    UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
     // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
     ug::HostStream hs{ug::make_stream(h.seed, ug::kNoiseTrial, (uint32_t)h.net_id, 0, trial), 0};
     const double mean_inj = 100.0 + ug::random_G(300.0, hs.word());
