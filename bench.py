@@ -428,7 +428,8 @@ def run_uneven(args, local_rank):
 
     one_round()   # first round: growth state set-up and graph capture
     sig = autotune.signature(_device_name(local_rank), [(n.n_ra, "growth", 1) for n in nets])
-    tuned = autotune.tune(eng, one_round, sig=sig, max_rounds=max(args.warmup, 6))
+    cache = autotune.DEFAULT_CACHE if args.autotune_cache is None else (args.autotune_cache or None)
+    tuned = autotune.tune(eng, one_round, sig=sig, max_rounds=max(args.warmup, 6), cache_path=cache)
     while trial[0] < args.warmup:
         one_round()
     l0 = eng.launch_count()
@@ -607,6 +608,8 @@ def main():
     ap.add_argument("--requests", type=int, default=48, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")
     ap.add_argument("--skip-sequential", action="store_true", help="uneven: skip the one-network-at-a-time timing")
+    ap.add_argument("--autotune-cache", default=None,
+                    help="uneven: autotuner cache file ('' to tune every run; default: the package's cache)")
     ap.add_argument("--batch", type=int, default=BATCH, help="test trials per step (profiling runs use fewer)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
