@@ -706,10 +706,11 @@ constexpr int kHeavyChunk = kHeavyWarps * 32 * kEvPerLane;   // events per block
 constexpr int kHeavyMinRows = 1024;                          // networks from this size take the block path
 
 struct HeavyShared {
-    double td[kHeavyChunk];
-    int tgt[kHeavyChunk];
-    double prev_td, Tsp;
-    int prev_t, first, ndue, unsorted, mode, slot, spk, head, num, cur, len, rem, sc;
+    double td[2][kHeavyChunk];   // the due events of a pass, by pass parity
+    int tgt[2][kHeavyChunk];
+    int first[2], ndue[2], unsorted[2];   // per-pass reductions, by pass parity
+    double Tsp;
+    int mode, slot, spk, head, num, cur, len;
 };
 
 // Block: queued row i of instance b in the interval s0..s1 (sh_T = T[s0..s1]).
@@ -766,33 +767,32 @@ __device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>&
                 hs.Tsp = n.T[stS[slot]];
                 hs.cur = stC[slot];
                 hs.len = stL[slot];
-                hs.prev_td = -1e300;
-                hs.prev_t = -1;
+                for (int p = 0; p < 2; ++p) {
+                    hs.first[p] = kHeavyChunk;
+                    hs.ndue[p] = 0;
+                    hs.unsorted[p] = 0;
+                }
             }
         }
         __syncwarp();
     }
     __syncthreads();
     if (hs.mode) {
+        // Two block barriers per pass: the per-pass reductions and event buffers
+        // alternate by pass parity, and every thread keeps the cursor itself.
         const double Tsp = hs.Tsp;
-        const int spk = hs.spk;
+        const int spk = hs.spk, len = hs.len, slot = hs.slot;
         const double* Tseg = sh_T + (from - s0);
-        while (true) {
-            if (threadIdx.x == 0) {
-                hs.first = kHeavyChunk;
-                hs.ndue = 0;
-                hs.unsorted = 0;
-                hs.rem = g.remodeled[r];
-                hs.sc = g.sup_cnt[r];
-            }
-            __syncthreads();
-            const int cur = hs.cur, len = hs.len, rem = hs.rem, sc = hs.sc;
+        int cur = hs.cur;
+        double prev_td = -1e300;
+        int prev_t = -1;
+        for (int p = 0;; p ^= 1) {
+            const int rem = g.remodeled[r], sc = g.sup_cnt[r];
             RowEv v[kEvPerLane];
-            int due_here = 0;
+            double tdk[kEvPerLane];
 #pragma unroll
             for (int k = 0; k < kEvPerLane; ++k) {
-                const int e = w * 32 * kEvPerLane + k * 32 + lane;   // position in the pass
-                const int idx = cur + e;
+                const int idx = cur + w * 32 * kEvPerLane + k * 32 + lane;
                 int t = -1;
                 double td = 0.0;
                 bool due = false;
@@ -801,55 +801,67 @@ __device__ __forceinline__ void g_row_heavy(const GrowthDev& g, const NetDev<R>&
                     td = Tsp + Drow[t];
                     due = Tlim >= td;
                 }
+                tdk[k] = td;
                 g_eval_ev(g, n, b, i, from, Tseg, due, td, t, spk, rem, sc, v[k]);
-                if (due) {
-                    hs.td[e] = td;
-                    hs.tgt[e] = t;
+            }
+            int due_here = 0;
+#pragma unroll
+            for (int k = 0; k < kEvPerLane; ++k) {
+                const int e = w * 32 * kEvPerLane + k * 32 + lane;   // position in the pass
+                if (v[k].has) {
+                    hs.td[p][e] = tdk[k];
+                    hs.tgt[p][e] = v[k].t;
                     ++due_here;
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, due && v[k].changing);
-                if (m && lane == 0) atomicMin(&hs.first, w * 32 * kEvPerLane + k * 32 + __ffs(m) - 1);
+                const unsigned m = __ballot_sync(0xffffffffu, v[k].has && v[k].changing);
+                if (m && lane == 0) atomicMin(&hs.first[p], w * 32 * kEvPerLane + k * 32 + __ffs(m) - 1);
             }
             // due events are a prefix of the stream: their count is the prefix length
             for (int o = 16; o > 0; o >>= 1) due_here += __shfl_xor_sync(0xffffffffu, due_here, o);
-            if (lane == 0) atomicAdd(&hs.ndue, due_here);
+            if (lane == 0) atomicAdd(&hs.ndue[p], due_here);
             __syncthreads();
-            const int ndue = hs.ndue;
+            const int ndue = hs.ndue[p];
             // the prefix must be in (time, target) order, continuing the previous pass
             for (int e = threadIdx.x; e < ndue; e += blockDim.x) {
-                const double ta = e ? hs.td[e - 1] : hs.prev_td;
-                const int ga = e ? hs.tgt[e - 1] : hs.prev_t;
-                if (!(ta < hs.td[e] || (ta == hs.td[e] && ga < hs.tgt[e]))) hs.unsorted = 1;
+                const double ta = e ? hs.td[p][e - 1] : prev_td;
+                const int ga = e ? hs.tgt[p][e - 1] : prev_t;
+                if (!(ta < hs.td[p][e] || (ta == hs.td[p][e] && ga < hs.tgt[p][e]))) hs.unsorted[p] = 1;
+            }
+            if (threadIdx.x == 0) {   // the next pass's reductions (last read a pass ago)
+                hs.first[p ^ 1] = kHeavyChunk;
+                hs.ndue[p ^ 1] = 0;
+                hs.unsorted[p ^ 1] = 0;
             }
             __syncthreads();
-            if (hs.unsorted) break;   // the warp path takes over from cur
-            const int f = min(hs.first, ndue);
+            if (hs.unsorted[p]) break;   // the warp path takes over from cur
+            const int f = min(hs.first[p], ndue);
 #pragma unroll
             for (int k = 0; k < kEvPerLane; ++k) {
                 const int e = w * 32 * kEvPerLane + k * 32 + lane;
                 if (v[k].has && e < f) g_commit(g, n, bt, b, v[k]);
             }
-            __syncthreads();
-            if (threadIdx.x == 0 && f < ndue) {
-                // the first event that can change the row: alone, then re-evaluate after it
-                const double tdf = hs.td[f];
-                int sd = from;
-                while (Tseg[sd - from] < tdf) ++sd;
-                g_deliver(g, n, bt, b, i, hs.tgt[f], sd, spk, tdf);
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                const int adv = f < ndue ? f + 1 : ndue;
-                if (adv > 0) {
-                    hs.prev_td = hs.td[adv - 1];
-                    hs.prev_t = hs.tgt[adv - 1];
+            if (f < ndue) {
+                // the first event that can change the row: alone, after the others'
+                // commits, then evaluation restarts after it
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    const double tdf = hs.td[p][f];
+                    int sd = from;
+                    while (Tseg[sd - from] < tdf) ++sd;
+                    g_deliver(g, n, bt, b, i, hs.tgt[p][f], sd, spk, tdf);
                 }
-                hs.cur = cur + adv;
-                stC[hs.slot] = hs.cur;
+                __syncthreads();
             }
-            __syncthreads();
+            const int adv = f < ndue ? f + 1 : ndue;
+            if (adv > 0) {
+                prev_td = hs.td[p][adv - 1];
+                prev_t = hs.tgt[p][adv - 1];
+            }
+            cur += adv;
             if (f >= ndue && ndue < kHeavyChunk) break;
         }
+        __syncthreads();   // every commit before the warp path continues
+        if (threadIdx.x == 0) stC[slot] = cur;
     }
     __syncthreads();
     if (w == 0) {
