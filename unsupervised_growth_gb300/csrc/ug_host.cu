@@ -282,6 +282,7 @@ private:
     std::vector<int> syncidx_;
     std::vector<double> ra_decay_, i_decay_;
     double max_delay_ = 0.0;   // bound on every delay, including those a replaced neuron can get
+    double delay_spread_ = -1.0;   // routing of group rows (member()); < 0: not computed yet
 };
 
 template <class R>
@@ -955,7 +956,19 @@ ug_status NetImpl<R>::member(ug::GroupMember<R>* m, int index, int2* act_rows, i
         m->bt.act_cnt = act_cnt;
         m->bt.act_cap = act_cap;
         m->bt.live_streams = gd_.st_num;
-        m->bt.heavy = h.n_ra >= ug::kHeavyMinRows ? 1 : 0;
+        // Large networks take the block path for the rows that spiked; when the
+        // delays are short for the network's size, a row's later intervals also
+        // carry hundreds of due events, and every queued row takes it.
+        if (h.n_ra >= ug::kHeavyMinRows) {
+            if (delay_spread_ < 0.0) {   // about the delay range: twice the mean of a sample
+                double sum = 0.0;
+                size_t cnt = 0;
+                const size_t nn = h.D.size(), stride = std::max<size_t>(1, nn / 65536);
+                for (size_t k = 0; k < nn; k += stride, ++cnt) sum += h.D[k];
+                delay_spread_ = std::max(2.0 * sum / (double)std::max<size_t>(cnt, 1), 0.25);
+            }
+            m->bt.heavy = (double)h.n_ra * 0.25 / delay_spread_ > 256.0 ? 2 : 1;
+        }
     }
     return UG_OK;
 }

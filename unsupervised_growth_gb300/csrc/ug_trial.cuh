@@ -93,7 +93,7 @@ struct BatchDev {
     int act_cap;
     int member;                // index of this batch in its group
     const int* live_streams;   // [B][n_ra] open delivery streams of each row (the growth state)
-    int heavy;                 // the rows take the heavy (block) path
+    int heavy;                 // block path: 0 never, 1 rows that spiked, 2 every queued row
 };
 
 // Queues row x of a group growth member for interval q if it has deliveries to make.
@@ -101,7 +101,8 @@ template <class R>
 __device__ __forceinline__ void queue_row(const BatchDev<R>& bt, int q, int x, uint32_t soma)
 {
     if (!soma && bt.live_streams[x] == 0) return;
-    const int list = (bt.heavy ? 2 : 0) + (q & 1);
+    const bool block = bt.heavy == 2 || (bt.heavy == 1 && soma != 0);
+    const int list = (block ? 2 : 0) + (q & 1);
     const int pos = atomicAdd(&bt.act_cnt[list], 1);
     if (pos < bt.act_cap) bt.act_rows[(size_t)list * bt.act_cap + pos] = make_int2(bt.member, x);
     else atomicOr(bt.error, kErrEventCapacity);
