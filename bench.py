@@ -572,6 +572,64 @@ def run_serve(args, local_rank):
     return res
 
 
+def run_topology(args, local_rank):
+    """Single precision against the double build over consecutive growth trials of
+    the 2000/550 growth network: per trial, the grown supersynapse and active
+    topology, the weights and the spikes; reports the first trial whose topology
+    differs, if any.  A step is one growth trial of both builds."""
+    import numpy as np
+
+    from tests.helpers import match_within, sorted_spikes
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    B.build()
+    net = make_growth_network()
+    e32, e64 = Engine(precision=32, device=local_rank), Engine(precision=64, device=local_rank)
+    r32, r64 = e32.load_network(net), e64.load_network(net)
+    first_div = {"super": None, "active": None}
+    worst_w, worst_rel, min_match, worst_step, spikes = 0.0, 0.0, 1.0, 0, 0
+    t32 = t64 = 0.0
+    for t in range(args.steps):
+        t0 = time.perf_counter()
+        r32.run_growth_trials(t, 1, True)
+        e32.synchronize()
+        t32 += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        r64.run_growth_trials(t, 1, True)
+        e64.synchronize()
+        t64 += time.perf_counter() - t0
+        for which, key in ((1, "super"), (0, "active")):
+            a = [sorted(x) for x in r32.synapse_list(which)]
+            b = [sorted(x) for x in r64.synapse_list(which)]
+            if a != b and first_div[key] is None:
+                first_div[key] = t
+        w32, w64 = r32.weights(), r64.weights()
+        d = np.abs(w32 - w64)
+        worst_w = max(worst_w, float(d.max()))
+        worst_rel = max(worst_rel, float((d / np.maximum(np.abs(w64), 1e-300))[w64 != 0].max(initial=0.0)))
+        a, b = sorted_spikes(*r32.spikes(0, 0)), sorted_spikes(*r64.spikes(0, 0))
+        frac, worst = match_within(a, b, 1)
+        spikes += len(b)
+        min_match, worst_step = min(min_match, frac), max(worst_step, worst)
+    sup = sum(len(x) for x in r64.synapse_list(1))
+    res = {"metric": "growth topology agreement, single vs double precision (consecutive growth trials)",
+           "value": args.steps if first_div["super"] is None else first_div["super"], "unit": "trials",
+           "n_gpus": 1, "steps": args.steps, "warmup": 0, "higher_is_better": True,
+           "dtype": "f32 neurons, f64 weights vs f64", "data": "synthetic (seeded network and Philox noise)",
+           "config": {"workload": "growth trials of one 2000 HVC-RA + 550 HVC-I sphere network, lognormal delays "
+                                  "mean 3 ms capped 10 ms, 10 training neurons"},
+           "first_divergent_trial": first_div, "supersynapses_at_end": sup,
+           "max_weight_abs_error": worst_w, "max_weight_rel_error": worst_rel,
+           "soma_spikes_fp64": spikes, "min_fraction_matched_within_1_step": min_match, "max_step_error": worst_step,
+           "s_per_trial": {"f32": t32 / args.steps, "f64": t64 / args.steps},
+           "value_means": "trials before the supersynapse topology first differs (= steps if never)"}
+    for r in (r32, r64):
+        r.free()
+    e32.close()
+    e64.close()
+    return res
+
+
 def run_reference(args, rank):
     if rank != 0:
         return None
@@ -600,10 +658,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="test", choices=["test", "growth", "uneven", "serve"],
+    ap.add_argument("--workload", default="test", choices=["test", "growth", "uneven", "serve", "topology"],
                     help="test: batched test trials (the headline); growth: consecutive growth trials of one "
                          "network; uneven: one group of growing networks of uneven size; serve: a Poisson stream "
-                         "of requests through the serving loop")
+                         "of requests through the serving loop; topology: single vs double precision over "
+                         "consecutive growth trials")
     ap.add_argument("--members", type=int, default=64, help="uneven: networks in the group; serve: member slots")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")
@@ -626,6 +685,8 @@ def main():
         res = run_uneven(args, local_rank) if rank == 0 else None
     elif args.workload == "serve":
         res = run_serve(args, local_rank) if rank == 0 else None
+    elif args.workload == "topology":
+        res = run_topology(args, local_rank) if rank == 0 else None
     else:
         res = run_ours(args, rank, world, local_rank)
     if rank == 0 and res is not None:
