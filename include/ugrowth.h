@@ -212,6 +212,50 @@ ug_status ug_get_connections(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t
                              double* weights, double* delays, int64_t* total);
 /* Neuron positions on the unit sphere, [n_ra][3] and [n_i][3]. */
 ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double* i_xyz);
+/* Lengths of the RA->I (which 0) or I->RA (which 1) connections (syn_lengths_*), in the
+ * order of ug_get_connections' targets. */
+ug_status ug_get_connection_lengths(ug_ctx* ctx, int32_t net_id, int32_t which, double* lengths);
+
+/* Sizes and parameters of a loaded network. */
+typedef struct {
+    int32_t n_ra, n_i, num_steps, n_tr;
+    uint64_t seed;
+    int32_t net_id;
+    int32_t batch;              /* instances of the last batch (0: none has run) */
+    ug_synaptic_params syn;
+    ug_maturation_params mat;
+    ug_noise_params noise;
+    ug_connection_params conn;
+} ug_network_info;
+ug_status ug_get_network_info(ug_ctx* ctx, int32_t net_id, ug_network_info* info);
+/* Spike counts of the last RATE_WINDOW_LONG growth trials per HVC(RA) neuron, newest first,
+ * [n_ra][RATE_WINDOW_LONG] (num_spikes_in_recent_trials, NetworkGrowthSimulator.h:253). */
+ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out);
+/* Training neurons and their spread times, [n_tr] each. */
+ug_status ug_get_training(ug_ctx* ctx, int32_t net_id, int32_t* neurons, double* spread);
+
+/* Reference directory formats.  read_network_state (NetworkGrowthSimulator.cpp:1943-2020):
+ * loads the state files of `dir` for `starting_trial` ("_<trial>" suffix when > 0) and its
+ * growth_parameters.cfg / network_parameters.cfg; num_steps 0 means 25000 (a 500 ms trial).
+ * The noise streams are those of (seed, stream_id). */
+ug_status ug_load_network_dir(ug_ctx* ctx, const char* dir, int32_t starting_trial, int32_t num_steps,
+                              uint64_t seed, int32_t stream_id, int32_t* net_id);
+/* write_full_network_state (NetworkGrowthSimulator.cpp:18552-18593): the state files, with
+ * file_ending appended to their names, the spike times of the last trial (instance 0), and
+ * one record appended to weight_statistics.bin (started anew when trial_number is 0). */
+ug_status ug_write_state_dir(ug_ctx* ctx, int32_t net_id, const char* dir, const char* file_ending,
+                             int32_t trial_number);
+/* write_network_topology (NetworkGrowthSimulator.cpp:18294-18310) plus the training files
+ * (:18502-18538): I_xy, RA_xy, RA_I / I_RA connections, num_neurons, training neurons and
+ * spread. */
+ug_status ug_write_topology_dir(ug_ctx* ctx, int32_t net_id, const char* dir);
+/* write_num_synapses / write_replaced_neurons (:17859-17914): append one record for
+ * trial_number (the file starts anew when trial_number is 0). */
+ug_status ug_append_num_synapses(ug_ctx* ctx, int32_t net_id, const char* path, int32_t trial_number);
+ug_status ug_append_replaced(ug_ctx* ctx, int32_t net_id, const char* path, int32_t trial_number);
+/* calculate_and_write_jitter (NetworkGrowthSimulator.cpp:1641-1735, write_jitter :17818-17857)
+ * over every trial of the last test batch. */
+ug_status ug_write_jitter(ug_ctx* ctx, int32_t net_id, const char* path);
 
 /* Per-instance spike statistics of the last batch: count and first step per neuron,
  * arrays [n_trials][n].  which: 0 somatic (HVC-RA), 1 dendritic (HVC-RA), 2 HVC-I. */

@@ -22,7 +22,8 @@ EXTRA = os.environ.get("UG_NVCC_EXTRA", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
-UNITS = [("ug_kernels_f64.cu", ["-fmad=false"]), ("ug_kernels_f32.cu", []), ("ug_host.cu", []), ("ug_calib.cu", [])]
+UNITS = [("ug_kernels_f64.cu", ["-fmad=false"]), ("ug_kernels_f32.cu", []), ("ug_host.cu", []), ("ug_calib.cu", []),
+         ("ug_files.cpp", [])]
 
 
 def nvcc() -> str:
@@ -33,7 +34,7 @@ def nvcc() -> str:
 
 
 def _sources():
-    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h"))] + [
+    return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h", ".cpp"))] + [
         os.path.join(ROOT, "include", "ugrowth.h")]
 
 
@@ -52,7 +53,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def compile_unit(unit):
         src, extra = unit
-        obj = os.path.join(OUT_DIR, src.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
         cmd = [nvcc()] + ARCH + COMMON + EXTRA + extra + ["-c", os.path.join(CSRC, src), "-o", obj]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)

@@ -36,6 +36,13 @@ ug_status fail(ug_status s, const std::string& msg)
     return s;
 }
 
+}  // namespace
+
+// The message ug_last_error returns, for the other translation units of the library.
+void ug_set_last_error(const std::string& msg) { g_err = msg; }
+
+namespace {
+
 #define UG_CUDA(call)                                                                          \
     do {                                                                                       \
         cudaError_t e_ = (call);                                                               \
@@ -163,6 +170,7 @@ public:
     // for double-precision networks or when growth trials changed the RA->RA lists
     // since they were last uploaded.
     virtual bool f32_view(ug::NetDev<float>* out) const { (void)out; return false; }
+    virtual int batch() const = 0;   // instances of the last batch
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -233,6 +241,7 @@ public:
     // loaded and run as `kind` (0 test, 1 growth) with B instances.
     size_t device_bytes() const;
     size_t footprint(int kind, int B) const;
+    int batch() const override { return B_; }
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -2052,6 +2061,68 @@ ug_status ug_get_coordinates(ug_ctx* ctx, int32_t net_id, double* ra_xyz, double
     UG_TRY(get_net(ctx, net_id, &n));
     if (ra_xyz) std::copy(n->h.ra_xyz.begin(), n->h.ra_xyz.end(), ra_xyz);
     if (i_xyz) std::copy(n->h.i_xyz.begin(), n->h.i_xyz.end(), i_xyz);
+    return UG_OK;
+}
+
+ug_status ug_get_connection_lengths(ug_ctx* ctx, int32_t net_id, int32_t which, double* lengths)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (which != 0 && which != 1) return fail(UG_EINVAL, "which must be 0 (RA->I) or 1 (I->RA)");
+    const std::vector<double>& L = which == 0 ? n->h.ra2i_len : n->h.i2ra_len;
+    if (lengths) std::copy(L.begin(), L.end(), lengths);
+    return UG_OK;
+}
+
+ug_status ug_get_network_info(ug_ctx* ctx, int32_t net_id, ug_network_info* info)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (!info) return fail(UG_EINVAL, "null output");
+    std::memset(info, 0, sizeof(*info));
+    info->n_ra = n->h.n_ra;
+    info->n_i = n->h.n_i;
+    info->num_steps = n->h.num_steps;
+    info->n_tr = (int32_t)n->h.training.size();
+    info->seed = n->h.seed;
+    info->net_id = n->h.net_id;
+    info->batch = n->batch();
+    info->syn = n->h.syn;
+    info->mat = n->h.mat;
+    info->noise = n->h.noise;
+    info->conn = n->h.conn;
+    return UG_OK;
+}
+
+ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (!out) return fail(UG_EINVAL, "null output");
+    const int W = n->h.mat.RATE_WINDOW_LONG;
+    if (W <= 0) return UG_OK;
+    for (int i = 0; i < n->h.n_ra; ++i)
+        for (int k = 0; k < W; ++k)
+            out[(size_t)i * W + k] = n->h.hist[(size_t)i * W + (n->h.hist_head + k) % W];
+    return UG_OK;
+}
+
+ug_status ug_get_training(ug_ctx* ctx, int32_t net_id, int32_t* neurons, double* spread)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    for (size_t k = 0; k < n->h.training.size(); ++k) {
+        if (neurons) neurons[k] = n->h.training[k];
+        if (spread) spread[k] = n->h.spread[n->h.training[k]];
+    }
     return UG_OK;
 }
 

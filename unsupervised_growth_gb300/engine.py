@@ -26,7 +26,9 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_launch",
             "ug_server_start", "ug_submit", "ug_poll", "ug_server_stop", "ug_get_weights", "ug_get_delays",
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
-            "ug_get_coordinates", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
+            "ug_get_coordinates", "ug_get_connection_lengths", "ug_get_network_info", "ug_get_activity_history",
+            "ug_get_training", "ug_load_network_dir", "ug_write_state_dir", "ug_write_topology_dir",
+            "ug_append_num_synapses", "ug_append_replaced", "ug_write_jitter", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
             "ug_run_test_trial_noalloc", "ug_calibrate_pipes"]
 
@@ -78,6 +80,12 @@ class NetworkDesc(C.Structure):
                 ("ra_xyz", _f64p), ("i_xyz", _f64p)]
 
 
+class NetworkInfo(C.Structure):
+    _fields_ = [("n_ra", C.c_int32), ("n_i", C.c_int32), ("num_steps", C.c_int32), ("n_tr", C.c_int32),
+                ("seed", C.c_uint64), ("net_id", C.c_int32), ("batch", C.c_int32), ("syn", SynapticParams),
+                ("mat", MaturationParams), ("noise", NoiseParams), ("conn", ConnectionParams)]
+
+
 class RuntimeOpts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("spike_capacity_per_neuron", C.c_int32),
                 ("use_graphs", C.c_int32)]
@@ -127,6 +135,16 @@ def load_library(path: str = LIB_PATH):
     L.ug_free_network.argtypes = [vp, C.c_int32]
     L.ug_run_test_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32]
     L.ug_get_trial_stats.argtypes = [vp, C.c_int32, C.c_int32, _i32p, _i32p]
+    L.ug_get_connection_lengths.argtypes = [vp, C.c_int32, C.c_int32, _f64p]
+    L.ug_get_network_info.argtypes = [vp, C.c_int32, C.POINTER(NetworkInfo)]
+    L.ug_get_activity_history.argtypes = [vp, C.c_int32, _i32p]
+    L.ug_get_training.argtypes = [vp, C.c_int32, _i32p, _f64p]
+    L.ug_load_network_dir.argtypes = [vp, C.c_char_p, C.c_int32, C.c_int32, C.c_uint64, C.c_int32, _i32p]
+    L.ug_write_state_dir.argtypes = [vp, C.c_int32, C.c_char_p, C.c_char_p, C.c_int32]
+    L.ug_write_topology_dir.argtypes = [vp, C.c_int32, C.c_char_p]
+    L.ug_append_num_synapses.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
+    L.ug_append_replaced.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
+    L.ug_write_jitter.argtypes = [vp, C.c_int32, C.c_char_p]
     L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
     L.ug_run_group.argtypes = [vp, C.POINTER(GroupItem), C.c_int32]
     L.ug_set_group_launch.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
@@ -265,6 +283,44 @@ class ResidentNetwork:
         _check(self.engine.L.ug_step_time(self.engine.ctx, self.id, step, C.byref(t)))
         return t.value
 
+    def info(self) -> dict:
+        x = NetworkInfo()
+        _check(self.engine.L.ug_get_network_info(self.engine.ctx, self.id, C.byref(x)))
+        return dict(n_ra=x.n_ra, n_i=x.n_i, num_steps=x.num_steps, n_tr=x.n_tr, seed=x.seed, net_id=x.net_id,
+                    batch=x.batch, model_interneuron_distance=x.conn.model_interneuron_distance,
+                    rate_window=x.mat.RATE_WINDOW_LONG)
+
+    def activity_history(self):
+        """[n_ra][RATE_WINDOW_LONG] spike counts of the recent growth trials, newest first."""
+        w = self.info()["rate_window"]
+        out = np.zeros((self.n_ra, max(w, 0)), dtype=np.int32)
+        _check(self.engine.L.ug_get_activity_history(self.engine.ctx, self.id, _p(out, _i32p)))
+        return out
+
+    def connection_lengths(self, which: int):
+        n = len(self.connections(which)[1])
+        out = np.zeros(max(n, 1))
+        _check(self.engine.L.ug_get_connection_lengths(self.engine.ctx, self.id, which, _p(out, _f64p)))
+        return out[:n]
+
+    def write_state_dir(self, directory: str, trial_number: int, file_ending: str | None = None):
+        """The files write_full_network_state writes (suffix "_<trial>" by default when trial > 0)."""
+        e = file_ending if file_ending is not None else (f"_{trial_number}" if trial_number > 0 else "")
+        _check(self.engine.L.ug_write_state_dir(self.engine.ctx, self.id, directory.encode(), e.encode(),
+                                                trial_number))
+
+    def write_topology_dir(self, directory: str):
+        _check(self.engine.L.ug_write_topology_dir(self.engine.ctx, self.id, directory.encode()))
+
+    def append_num_synapses(self, path: str, trial_number: int):
+        _check(self.engine.L.ug_append_num_synapses(self.engine.ctx, self.id, path.encode(), trial_number))
+
+    def append_replaced(self, path: str, trial_number: int):
+        _check(self.engine.L.ug_append_replaced(self.engine.ctx, self.id, path.encode(), trial_number))
+
+    def write_jitter(self, path: str):
+        _check(self.engine.L.ug_write_jitter(self.engine.ctx, self.id, path.encode()))
+
     def free(self):
         if self.id is not None:
             _check(self.engine.L.ug_free_network(self.engine.ctx, self.id))
@@ -358,6 +414,17 @@ class Engine:
         rn = ResidentNetwork(self, net, net_id)
         rn.batch = n_trials if kind == "test" else 1
         return rn
+
+    def load_network_dir(self, directory: str, starting_trial: int = 0, num_steps: int = 0, seed: int = 15000,
+                         stream_id: int = 0) -> ResidentNetwork:
+        """A network from a directory in the reference's state format (read_network_state)."""
+        nid = C.c_int32(-1)
+        _check(self.L.ug_load_network_dir(self.ctx, directory.encode(), starting_trial, num_steps, seed, stream_id,
+                                          C.byref(nid)))
+        x = NetworkInfo()
+        _check(self.L.ug_get_network_info(self.ctx, nid.value, C.byref(x)))
+        net = Network(n_ra=x.n_ra, n_i=x.n_i, seed=seed, num_steps=x.num_steps, net_id=stream_id)
+        return ResidentNetwork(self, net, nid.value)
 
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
