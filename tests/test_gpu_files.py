@@ -58,41 +58,41 @@ def assert_same_state(a, b):
 def test_state_dir_round_trip_and_resume(engine32, tmp_path):
     eng, net = engine32, grown_net()
     a = eng.load_network(net)
-    a.run_growth_trials(0, 2, True)
+    a.run_growth_trials(0, 4, True)
     d, d2 = str(tmp_path / "state"), str(tmp_path / "again")
     os.makedirs(d)
     os.makedirs(d2)
     write_cfgs(d, net)
     a.write_topology_dir(d)
-    a.write_state_dir(d, 2)
-    b = eng.load_network_dir(d, 2, num_steps=net.num_steps, seed=net.seed, stream_id=net.net_id)
+    a.write_state_dir(d, 4)
+    b = eng.load_network_dir(d, 4, num_steps=net.num_steps, seed=net.seed, stream_id=net.net_id)
     sa = snapshot(a)
     assert_same_state(sa, snapshot(b))
-    assert sum(len(x) for x in sa["sup"]) > 0 and sa["props"]["trials_after_replacement"][5] == 1
+    assert sum(len(x) for x in sa["act"]) > 0 and sa["props"]["trials_after_replacement"][5] == 3
     # the same bytes when written again (the spike files need a trial of their own)
     b.write_topology_dir(d2)
-    b.write_state_dir(d2, 2)
+    b.write_state_dir(d2, 4)
     for name in sorted(os.listdir(d2)):
         if name.startswith("spike_times"):
             continue
         with open(os.path.join(d, name), "rb") as f1, open(os.path.join(d2, name), "rb") as f2:
             assert f1.read() == f2.read(), name
     # the library's files, read by the Python format module
-    W, trial = F.read_weights(os.path.join(d, "weights_2.bin"))
-    assert trial == 2 and np.array_equal(W, sa["W"])
-    assert F.read_synapse_lists(os.path.join(d, "RA_RA_super_connections_2.bin"))[0] == sa["sup"]
-    props, _ = F.read_maturation_properties(os.path.join(d, "maturation_properties_2.bin"))
+    W, trial = F.read_weights(os.path.join(d, "weights_4.bin"))
+    assert trial == 4 and np.array_equal(W, sa["W"])
+    assert F.read_synapse_lists(os.path.join(d, "RA_RA_super_connections_4.bin"))[0] == sa["sup"]
+    props, _ = F.read_maturation_properties(os.path.join(d, "maturation_properties_4.bin"))
     assert np.array_equal(props["maturation_scale"], sa["props"]["maturation_scale"].astype(np.int32))
-    assert np.array_equal(F.read_activity_history(os.path.join(d, "activity_history_2.bin"))[0], sa["hist"])
-    times, trial, dur = F.read_spike_times(os.path.join(d, "spike_times_soma_2.bin"))
+    assert np.array_equal(F.read_activity_history(os.path.join(d, "activity_history_4.bin"))[0], sa["hist"])
+    times, trial, dur = F.read_spike_times(os.path.join(d, "spike_times_soma_4.bin"))
     n, s = a.spikes(0, 0)
     want = [[a.step_time(int(st)) for nn, st in zip(n, s) if nn == i] for i in range(net.n_ra)]
-    assert trial == 2 and dur == 500.0 and [t.tolist() for t in times] == want
+    assert trial == 4 and dur == 500.0 and [t.tolist() for t in times] == want
     rec = np.fromfile(os.path.join(d, "weight_statistics.bin"), dtype=np.dtype([("t", "<i4"), ("m", "<f8"), ("s", "<f8")]))
-    assert len(rec) == 1 and rec["t"][0] == 2 and np.isclose(rec["m"][0], sa["W"].mean(), rtol=1e-13)
+    assert len(rec) == 1 and rec["t"][0] == 4 and np.isclose(rec["m"][0], sa["W"].mean(), rtol=1e-13)
     # resume: the next growth trial of both is the same
-    a.run_growth_trials(2, 1, True)
-    b.run_growth_trials(2, 1, True)
+    a.run_growth_trials(4, 1, True)
+    b.run_growth_trials(4, 1, True)
     assert_same_state(snapshot(a), snapshot(b))
     for w in (0, 1, 2):
         assert np.array_equal(sorted_spikes(*a.spikes(0, w)), sorted_spikes(*b.spikes(0, w))), w

@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(32 * kRowWarps) kl_growth_rows(const GroupMemb
 
 // One block per queued heavy row of interval q (spiking rows of large networks).
 template <class R>
-__global__ void __launch_bounds__(32 * kHeavyWarps, 2) kl_growth_rows_heavy(const GroupMember<R>* members,
+__global__ void __launch_bounds__(32 * kHeavyWarps, 1) kl_growth_rows_heavy(const GroupMember<R>* members,
                                                                          const int2* rows, const int* act_cnt,
                                                                          int act_cap, const double* T, int q, int s0,
                                                                          int s1)

@@ -701,7 +701,7 @@ __device__ __forceinline__ int g_row(const GrowthDev& g, const NetDev<R>& n, con
 // target) -- which the block checks pass by pass, handing the row back to the
 // warp path (and its ranked merge) at the first pass that is not.  Everything
 // before a spike of the row, and any remainder, goes through the warp path.
-constexpr int kHeavyWarps = 8;
+constexpr int kHeavyWarps = 16;
 constexpr int kHeavyChunk = kHeavyWarps * 32 * kEvPerLane;   // events per block pass
 constexpr int kHeavyMinRows = 1024;                          // networks from this size take the block path
 

@@ -190,6 +190,10 @@ cudaError_t group_grids(GroupDev& d, int ra_blocks_per_sm, int i_blocks_per_sm)
     d.grid[kListLtp] = occupancy(kl_growth_ltp<R>, kBlock, 0);
     d.grid[kListCheck] = occupancy(kl_check_bad<R>, 256, 0);
     d.grid[kNumLists] = occupancy(kl_growth_rows<R>, 32 * kRowWarps, kRowWarps * sizeof(RowShared));
+    // the heavy-row kernel's buffers exceed the default 48 KB of dynamic shared memory
+    e = cudaFuncSetAttribute(kl_growth_rows_heavy<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(RowShared) + sizeof(HeavyShared)));
+    if (e != cudaSuccess) return e;
     d.grid[kNumLists + 1] = occupancy(kl_growth_rows_heavy<R>, 32 * kHeavyWarps, sizeof(RowShared) + sizeof(HeavyShared));
     for (int k = 0; k <= kNumLists + 1; ++k)
         if (d.grid[k] <= 0) return cudaErrorInvalidConfiguration;
