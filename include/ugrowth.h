@@ -256,6 +256,23 @@ ug_status ug_append_replaced(ug_ctx* ctx, int32_t net_id, const char* path, int3
 /* calculate_and_write_jitter (NetworkGrowthSimulator.cpp:1641-1735, write_jitter :17818-17857)
  * over every trial of the last test batch. */
 ug_status ug_write_jitter(ug_ctx* ctx, int32_t net_id, const char* path);
+/* write_soma_spike_times / write_dend_spike_times / write_interneuron_spike_times
+ * (:17916-18033) for one instance of the last batch; which 0 soma, 1 dendrite, 2 HVC(I). */
+ug_status ug_write_spike_times(ug_ctx* ctx, int32_t net_id, int32_t instance, int32_t which, const char* path,
+                               int32_t trial_number);
+/* write_graph_network_state (:18620-18641): appends to num_synapses.bin, and writes the
+ * spike times of the last trial and the active and super synapse lists. */
+ug_status ug_write_graph_state(ug_ctx* ctx, int32_t net_id, const char* dir, int32_t trial_number);
+/* The set-up of new_chain_growth (NetworkGrowthSimulator.cpp:1865-1940): reads the topology
+ * directory (read_network_topology), the training neurons and the growth parameter file;
+ * computes the axonal delays from the lengths and the sphere positions (sample_axonal_delays),
+ * redraws the RA<->I weights uniformly below their maxima (resample_weights, from the
+ * (seed, stream_id) set-up stream), makes the training neurons mature; writes the files
+ * new_chain_growth writes into out_dir (parameter files, I_xy, training files, num_neurons,
+ * the "_initial" network), and loads the network. */
+ug_status ug_create_growth_network(ug_ctx* ctx, const char* network_dir, const char* training_file,
+                                   const char* config_file, const char* out_dir, int32_t num_steps, uint64_t seed,
+                                   int32_t stream_id, int32_t* net_id);
 
 /* Per-instance spike statistics of the last batch: count and first step per neuron,
  * arrays [n_trials][n].  which: 0 somatic (HVC-RA), 1 dendritic (HVC-RA), 2 HVC-I. */

@@ -17,11 +17,13 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.environ.get("UG_BUILD_DIR", os.path.join(HERE, "_lib"))
 LIB = os.path.join(OUT_DIR, "libugrowth.so")
+CLI = os.path.join(OUT_DIR, "ug_growth")   # the command-line programs (csrc/ug_cli.cpp)
 # extra nvcc flags, e.g. -DUG_RA_MIN_BLOCKS=4 to build a tuning variant into UG_BUILD_DIR
 EXTRA = os.environ.get("UG_NVCC_EXTRA", "").split()
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
+CLI_SRC = "ug_cli.cpp"
 UNITS = [("ug_kernels_f64.cu", ["-fmad=false"]), ("ug_kernels_f32.cu", []), ("ug_host.cu", []), ("ug_calib.cu", []),
          ("ug_files.cpp", [])]
 
@@ -62,14 +64,22 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=len(UNITS) + 1) as ex:
+        cli = ex.submit(compile_unit, (CLI_SRC, []))
         objs = list(ex.map(compile_unit, UNITS))
+        cli_obj = cli.result()
     tmp = LIB + ".tmp"
     cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the command-line programs, linked against the library next to them
+    cmd = [nvcc(), cli_obj, "-o", CLI + ".tmp", "-L" + OUT_DIR, "-lugrowth", "-Xlinker", "-rpath=$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link of {CLI} failed:\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

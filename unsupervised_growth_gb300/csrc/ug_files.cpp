@@ -7,6 +7,7 @@
 // ConfigurationNetworkTopology, of which this parser reads the subset they use
 // (groups of scalar settings, '=' or ':', quoted strings, comments).
 #include "ugrowth.h"
+#include "ug_philox.cuh"
 
 #include <algorithm>
 #include <cctype>
@@ -295,13 +296,14 @@ ug_status get_lists(ug_ctx* ctx, int32_t net, int which, int n, std::vector<int3
     return ug_get_synapse_list(ctx, net, which, off.data(), tgt.data(), &total);
 }
 
-ug_status write_spikes(ug_ctx* ctx, int32_t net, int which, int n, int32_t trial, const std::string& path)
+ug_status write_spikes(ug_ctx* ctx, int32_t net, int which, int n, int32_t trial, const std::string& path,
+                       int instance = 0)
 {
     int64_t cnt = 0;
     std::vector<int32_t> nid, step;
-    if (ug_get_spikes(ctx, net, 0, which, nullptr, nullptr, 0, &cnt) == UG_OK) {
+    if (ug_get_spikes(ctx, net, instance, which, nullptr, nullptr, 0, &cnt) == UG_OK) {
         nid.resize(cnt); step.resize(cnt);
-        UG_FTRY(ug_get_spikes(ctx, net, 0, which, nid.data(), step.data(), cnt, &cnt));
+        UG_FTRY(ug_get_spikes(ctx, net, instance, which, nid.data(), step.data(), cnt, &cnt));
     }   // a network that has run no trial writes empty lists
     std::vector<std::vector<double>> t(n);
     for (int64_t k = 0; k < cnt; ++k) {
@@ -710,4 +712,262 @@ ug_status ug_write_jitter(ug_ctx* ctx, int32_t net, const char* path)
     return closed(o, path);
 }
 
+ug_status ug_write_spike_times(ug_ctx* ctx, int32_t net, int32_t instance, int32_t which, const char* path,
+                               int32_t trial_number)
+{
+    if (!ctx || !path) return ferr(UG_EINVAL, "null argument");
+    if (which < 0 || which > 2) return ferr(UG_EINVAL, "which must be 0, 1 or 2");
+    ug_network_info info;
+    UG_FTRY(ug_get_network_info(ctx, net, &info));
+    if (instance < 0 || instance >= info.batch) return ferr(UG_EINVAL, "instance out of range");
+    return write_spikes(ctx, net, which, which == 2 ? info.n_i : info.n_ra, trial_number, path, instance);
+}
+
+ug_status ug_write_graph_state(ug_ctx* ctx, int32_t net, const char* dir_c, int32_t trial_number)
+{
+    if (!ctx || !dir_c) return ferr(UG_EINVAL, "null argument");
+    const std::string dir(dir_c);
+    ug_network_info info;
+    UG_FTRY(ug_get_network_info(ctx, net, &info));
+    const int n = info.n_ra;
+    UG_FTRY(ug_append_num_synapses(ctx, net, join(dir, "num_synapses.bin").c_str(), trial_number));
+    UG_FTRY(write_spikes(ctx, net, 0, n, trial_number, join(dir, "spike_times_soma.bin")));
+    UG_FTRY(write_spikes(ctx, net, 1, n, trial_number, join(dir, "spike_times_dend.bin")));
+    UG_FTRY(write_spikes(ctx, net, 2, info.n_i, trial_number, join(dir, "spike_times_interneuron.bin")));
+    for (int which = 1; which >= 0; --which) {
+        std::vector<int32_t> off, tgt;
+        UG_FTRY(get_lists(ctx, net, which, n, off, tgt));
+        const std::string p = join(dir, which ? "RA_RA_super_connections.bin" : "RA_RA_active_connections.bin");
+        Out o(p, false);
+        o.put((int32_t)n); o.put(trial_number);
+        for (int i = 0; i < n; ++i) {
+            o.put((int32_t)(off[i + 1] - off[i]));
+            o.put(tgt.data() + off[i], (size_t)(off[i + 1] - off[i]));
+        }
+        UG_FTRY(closed(o, p));
+    }
+    return UG_OK;
+}
+
 }  // extern "C"
+
+namespace {
+
+const char* const kSynFields[] = {"A_P", "A_D", "T_0", "T_P", "T_D", "TAU_P", "TAU_D", "BETA", "BETA_SUPERSYNAPSE",
+                                  "ACTIVATION_THRESHOLD", "SUPERSYNAPSE_THRESHOLD", "WEIGHT_MAX"};
+const char* const kMatFields[] = {"E_GABA_MATURE", "E_GABA_IMMATURE", "E_REST_MATURE", "E_REST_IMMATURE",
+                                  "AD_MATURE", "AD_IMMATURE", "GK_MATURE", "GK_IMMATURE", "GNA_MATURE",
+                                  "GNA_IMMATURE", "GCA_MATURE", "GCA_IMMATURE", "GCAK_MATURE", "GCAK_IMMATURE",
+                                  "GSL_MATURE", "GSL_IMMATURE", "GDL_MATURE", "GDL_IMMATURE", "RC_MATURE",
+                                  "RC_IMMATURE"};
+
+std::string fixed6(double v)
+{
+    char b[64];
+    std::snprintf(b, sizeof(b), "%.6f", v);
+    return b;
+}
+
+// ConfigurationNetworkGrowth::write_configuration (ConfigurationNetworkGrowth.cpp:210-295):
+// std::fixed with six decimals from A_P on, blank lines as it places them.
+ug_status write_growth_cfg(const std::string& path, const Cfg& c)
+{
+    auto v = [&](const char* g, const char* k) {
+        double x = 0.0;
+        c.num(g, k, x);
+        return x;
+    };
+    std::string o = "synapticParameters = \n{\n\tNss = " + std::to_string((long)v("synapticParameters", "Nss")) + ";\n\n";
+    for (const char* k : kSynFields) {
+        o += std::string("\t") + k + " = " + fixed6(v("synapticParameters", k)) + ";\n";
+        if (!std::strcmp(k, "TAU_D") || !std::strcmp(k, "BETA_SUPERSYNAPSE") || !std::strcmp(k, "WEIGHT_MAX")) o += "\n";
+    }
+    o += "};\n\nmaturationParameters = \n{\n";
+    for (const char* k : kMatFields) {
+        o += std::string("\t") + k + " = " + fixed6(v("maturationParameters", k)) + ";\n";
+        if (std::strstr(k, "_IMMATURE")) o += "\n";
+    }
+    o += "\tDEATH_RATE_THRESHOLD = " + fixed6(v("maturationParameters", "DEATH_RATE_THRESHOLD")) + ";\n\n";
+    o += "\tRATE_WINDOW_LONG = " + std::to_string((long)v("maturationParameters", "RATE_WINDOW_LONG")) + ";\n\n";
+    o += "};\n\nnoiseParameters = \n{\n";
+    for (const char* k : {"white_noise_mean_soma", "white_noise_std_soma", "white_noise_mean_dend", "white_noise_std_dend"})
+        o += std::string("\t") + k + " = " + fixed6(v("noiseParameters", k)) + ";\n";
+    o += "};\n\nconnectionParameters = \n{\n";
+    for (const char* k : {"Gei_max", "Gie_max", "delay_constant"})
+        o += std::string("\t") + k + " = " + fixed6(v("connectionParameters", k)) + ";\n";
+    o += "};\n\n";
+    std::ofstream f(path);
+    f << o;
+    return f ? UG_OK : ferr(UG_EIO, "cannot write " + path);
+}
+
+// ConfigurationNetworkTopology::write_configuration (ConfigurationNetworkTopology.cpp:64-82).
+ug_status write_topology_cfg(const std::string& path, const Cfg& c)
+{
+    std::string arrangement;
+    auto gi = c.groups.find("spatialParameters");
+    if (gi != c.groups.end() && gi->second.count("arrangement")) arrangement = gi->second.at("arrangement");
+    auto v = [&](const char* k) {
+        double x = 0.0;
+        c.num("spatialParameters", k, x);
+        return x;
+    };
+    std::string o = "spatialParameters = \n{\n\tarrangement = \"" + arrangement + "\";\n";
+    for (const char* k : {"A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA"})
+        o += std::string("\t") + k + " = " + fixed6(v(k)) + ";\n";
+    o += "\n};\n\n";
+    std::ofstream f(path);
+    f << o;
+    return f ? UG_OK : ferr(UG_EIO, "cannot write " + path);
+}
+
+double sphere_dist(const double* a, const double* b)
+{
+    const double t = a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+    return t > 1.0 ? 0.0 : std::acos(t);
+}
+
+}  // namespace
+
+extern "C" ug_status ug_create_growth_network(ug_ctx* ctx, const char* network_dir, const char* training_file,
+                                              const char* config_file, const char* out_dir_c, int32_t num_steps,
+                                              uint64_t seed, int32_t stream_id, int32_t* net_id)
+{
+    if (!ctx || !network_dir || !training_file || !config_file || !net_id) return ferr(UG_EINVAL, "null argument");
+    const std::string dir(network_dir), out_dir(out_dir_c ? out_dir_c : "");
+    Cfg g, t;
+    UG_FTRY(parse_cfg(config_file, g));
+    UG_FTRY(parse_cfg(join(dir, "network_parameters.cfg"), t));
+    int32_t nra = 0, ni = 0;
+    {
+        In in(join(dir, "num_neurons.bin"));
+        if (!in.ok() || !in.get(nra) || !in.get(ni) || nra <= 0 || ni < 0) return bad_file(in);
+    }
+    std::vector<double> ra_xyz, i_xyz;
+    double model = 0.0, model_i = 0.0;
+    UG_FTRY(read_coords(join(dir, "RA_xy.bin"), nra, ra_xyz, model));
+    UG_FTRY(read_coords(join(dir, "I_xy.bin"), ni, i_xyz, model_i));
+    Conn ri, ir;
+    UG_FTRY(read_connections(join(dir, "RA_I_connections.bin"), nra, ri.off, ri.tgt, ri.w, ri.len, ri.d));
+    UG_FTRY(read_connections(join(dir, "I_RA_connections.bin"), ni, ir.off, ir.tgt, ir.w, ir.len, ir.d));
+    std::vector<int32_t> training;
+    {
+        In in(training_file);
+        int32_t k = 0;
+        if (!in.ok() || !in.get(k) || k < 0 || !in.get(training, (size_t)k)) return bad_file(in);
+        std::sort(training.begin(), training.end());
+        for (int32_t id : training)
+            if (id < 0 || id >= nra) return ferr(UG_EINVAL, "training neuron out of range");
+    }
+    double dc = 0.0, gei = 0.0, gie = 0.0;
+    g.num("connectionParameters", "delay_constant", dc);
+    g.num("connectionParameters", "Gei_max", gei);
+    g.num("connectionParameters", "Gie_max", gie);
+    if (!(model > 0.0)) return ferr(UG_EINVAL, "RA_xy.bin holds no model interneuron distance");
+    // sample_axonal_delays: lengths on the sphere in microns (EXPERIMENTAL_INTERNEURON_DISTANCE 40),
+    // 0.01 ms per micron times the delay constant
+    std::vector<double> L((size_t)nra * nra, 0.0), D((size_t)nra * nra, 0.0);
+    for (int i = 0; i < nra; ++i)
+        for (int j = 0; j < nra; ++j) {
+            const double len = j != i ? sphere_dist(&ra_xyz[3 * i], &ra_xyz[3 * j]) * 40.0 / model : 0.0;
+            L[(size_t)i * nra + j] = len;
+            D[(size_t)i * nra + j] = len * 0.01 * dc;
+        }
+    for (size_t k = 0; k < ri.len.size(); ++k) ri.d[k] = ri.len[k] * 0.01 * dc;
+    for (size_t k = 0; k < ir.len.size(); ++k) ir.d[k] = ir.len[k] * 0.01 * dc;
+    // resample_weights: I->RA first, then RA->I, uniform below the maxima
+    ug::HostStream hs{ug::make_stream(seed, ug::kNoiseCreate, (uint32_t)stream_id, 0, 0), 0};
+    for (double& w : ir.w) w = ug::random_G(1.0, hs.word()) * gie;
+    for (double& w : ri.w) w = ug::random_G(1.0, hs.word()) * gei;
+    // neuron state: immature and spontaneous, the training neurons mature
+    double e_mat = 0, e_imm = 0, g_mat = 0, g_imm = 0, win_d = 0;
+    g.num("maturationParameters", "E_REST_MATURE", e_mat);
+    g.num("maturationParameters", "E_REST_IMMATURE", e_imm);
+    g.num("maturationParameters", "GCA_MATURE", g_mat);
+    g.num("maturationParameters", "GCA_IMMATURE", g_imm);
+    g.num("maturationParameters", "RATE_WINDOW_LONG", win_d);
+    const int win = (int)win_d;
+    std::vector<double> rest(nra, e_imm), gca(nra, g_imm), scale(nra, 100000.0), spread(training.size(), 0.0);
+    std::vector<int32_t> mature(nra, 0), remod(nra, 0), tar(nra, 0), hist((size_t)nra * std::max(win, 0), 0);
+    for (int32_t id : training) {
+        mature[id] = 1;
+        gca[id] = g_mat;
+        rest[id] = e_mat;
+    }
+    std::vector<double> W((size_t)nra * nra, 0.0);
+    std::vector<int32_t> act_off(nra + 1, 0), sup_off(nra + 1, 0), empty(1, 0);
+    // files new_chain_growth writes
+    if (!out_dir.empty()) {
+        UG_FTRY(write_topology_cfg(join(out_dir, "network_parameters.cfg"), t));
+        UG_FTRY(write_growth_cfg(join(out_dir, "growth_parameters.cfg"), g));
+        const std::string pi = join(out_dir, "I_xy.bin");
+        Out oi(pi, false);
+        write_coords(oi, ni, i_xyz, model);
+        UG_FTRY(closed(oi, pi));
+        const std::string pn = join(out_dir, "training_neurons.bin"), ps = join(out_dir, "training_spread.bin");
+        Out on(pn, false), os(ps, false);
+        on.put((int32_t)training.size());
+        on.put(training.data(), training.size());
+        os.put((int32_t)spread.size());
+        os.put(spread.data(), spread.size());
+        UG_FTRY(closed(on, pn));
+        UG_FTRY(closed(os, ps));
+        const std::string pnn = join(out_dir, "num_neurons.bin");
+        Out onn(pnn, false);
+        onn.put(nra); onn.put(ni);
+        UG_FTRY(closed(onn, pnn));
+        const std::string pr = join(out_dir, "RA_xy_initial.bin");
+        Out orr(pr, false);
+        write_coords(orr, nra, ra_xyz, model);
+        UG_FTRY(closed(orr, pr));
+        const std::string p1 = join(out_dir, "RA_I_connections_initial.bin"), p2 = join(out_dir, "I_RA_connections_initial.bin");
+        Out a(p1, false), b(p2, false);
+        write_connections(a, nra, ri.off, ri.tgt, ri.w, ri.len, ri.d);
+        write_connections(b, ni, ir.off, ir.tgt, ir.w, ir.len, ir.d);
+        UG_FTRY(closed(a, p1));
+        UG_FTRY(closed(b, p2));
+    }
+    ug_network_desc d;
+    std::memset(&d, 0, sizeof(d));
+    d.n_ra = nra; d.n_i = ni;
+    d.num_steps = num_steps > 0 ? num_steps : 25000;
+    d.net_id = stream_id;
+    d.seed = seed;
+    Cfg none;
+    auto num = [](const Cfg& c, const char* grp, const char* key) {
+        double v = 0.0;
+        c.num(grp, key, v);
+        return v;
+    };
+    d.syn.Nss = (int32_t)num(g, "synapticParameters", "Nss");
+    double* syn_vals[] = {&d.syn.A_P, &d.syn.A_D, &d.syn.T_0, &d.syn.T_P, &d.syn.T_D, &d.syn.TAU_P, &d.syn.TAU_D,
+                          &d.syn.BETA, &d.syn.BETA_SUPERSYNAPSE, &d.syn.ACTIVATION_THRESHOLD,
+                          &d.syn.SUPERSYNAPSE_THRESHOLD, &d.syn.WEIGHT_MAX};
+    for (int k = 0; k < 12; ++k) *syn_vals[k] = num(g, "synapticParameters", kSynFields[k]);
+    d.mat.E_REST_MATURE = e_mat; d.mat.E_REST_IMMATURE = e_imm; d.mat.GCA_MATURE = g_mat; d.mat.GCA_IMMATURE = g_imm;
+    d.mat.DEATH_RATE_THRESHOLD = num(g, "maturationParameters", "DEATH_RATE_THRESHOLD");
+    d.mat.RATE_WINDOW_LONG = win;
+    d.noise.white_noise_mean_soma = num(g, "noiseParameters", "white_noise_mean_soma");
+    d.noise.white_noise_std_soma = num(g, "noiseParameters", "white_noise_std_soma");
+    d.noise.white_noise_mean_dend = num(g, "noiseParameters", "white_noise_mean_dend");
+    d.noise.white_noise_std_dend = num(g, "noiseParameters", "white_noise_std_dend");
+    d.conn.Gei_max = gei; d.conn.Gie_max = gie; d.conn.delay_constant = dc;
+    d.conn.A_RA2I = num(t, "spatialParameters", "A_RA2I"); d.conn.SIGMA_RA2I = num(t, "spatialParameters", "SIGMA_RA2I");
+    d.conn.B_I2RA = num(t, "spatialParameters", "B_I2RA"); d.conn.SIGMA_I2RA = num(t, "spatialParameters", "SIGMA_I2RA");
+    d.conn.model_interneuron_distance = model;
+    d.ra2i_off = ri.off.data(); d.ra2i_tgt = ri.tgt.data(); d.ra2i_w = ri.w.data(); d.ra2i_d = ri.d.data();
+    d.ra2i_len = ri.len.data();
+    d.i2ra_off = ir.off.data(); d.i2ra_tgt = ir.tgt.data(); d.i2ra_w = ir.w.data(); d.i2ra_d = ir.d.data();
+    d.i2ra_len = ir.len.data();
+    d.w_rara = W.data(); d.d_rara = D.data(); d.len_rara = L.data();
+    d.active_off = act_off.data(); d.active_tgt = empty.data();
+    d.super_off = sup_off.data(); d.super_tgt = empty.data();
+    d.rest_potential = rest.data(); d.gca = gca.data();
+    d.mature = mature.data(); d.maturation_scale = scale.data();
+    d.remodeled = remod.data(); d.trials_after_replacement = tar.data();
+    d.activity_history = hist.data();
+    d.n_tr = (int32_t)training.size();
+    d.training = training.data(); d.training_spread = spread.data();
+    d.ra_xyz = ra_xyz.data(); d.i_xyz = i_xyz.data();
+    return ug_load_network(ctx, &d, net_id);
+}

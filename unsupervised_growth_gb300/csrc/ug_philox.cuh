@@ -27,7 +27,8 @@ enum NoiseKind : uint32_t {
     kNoiseRAWhite = 1,    // HVC(RA) white noise: 4 words per integration step
     kNoiseIPoisson = 2,   // HVC(I) Poisson conductance noise: sequential words
     kNoiseTrial = 3,      // per-trial network draws (mean training injection time)
-    kNoiseReplace = 4     // neuron replacement resampling
+    kNoiseReplace = 4,    // neuron replacement resampling
+    kNoiseCreate = 5      // network set-up draws (the growth CLI's weight resampling)
 };
 
 struct Philox4 { uint32_t x, y, z, w; };

@@ -28,7 +28,8 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_connection_lengths", "ug_get_network_info", "ug_get_activity_history",
             "ug_get_training", "ug_load_network_dir", "ug_write_state_dir", "ug_write_topology_dir",
-            "ug_append_num_synapses", "ug_append_replaced", "ug_write_jitter", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
+            "ug_append_num_synapses", "ug_append_replaced", "ug_write_jitter", "ug_write_spike_times",
+            "ug_write_graph_state", "ug_create_growth_network", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
             "ug_run_test_trial_noalloc", "ug_calibrate_pipes"]
 
@@ -145,6 +146,10 @@ def load_library(path: str = LIB_PATH):
     L.ug_append_num_synapses.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
     L.ug_append_replaced.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
     L.ug_write_jitter.argtypes = [vp, C.c_int32, C.c_char_p]
+    L.ug_write_spike_times.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_char_p, C.c_int32]
+    L.ug_write_graph_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
+    L.ug_create_growth_network.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_int32,
+                                           C.c_uint64, C.c_int32, _i32p]
     L.ug_run_growth_trials.argtypes = [vp, C.c_int32, C.c_uint32, C.c_int32, C.c_int32]
     L.ug_run_group.argtypes = [vp, C.POINTER(GroupItem), C.c_int32]
     L.ug_set_group_launch.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
