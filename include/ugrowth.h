@@ -311,6 +311,57 @@ ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint32_t trial,
                                     int32_t* soma_first, int32_t* dend_count, int32_t* dend_first,
                                     int32_t* inter_count, int32_t* inter_first);
 
+/* ---- Network topology generation (createNetworkForGrowth) ----------------------------
+ * generate_network_topology (NetworkGrowthSimulator.cpp:110-155) on the device:
+ * sample_coordinates (:222-403), sample_connections (:620-705) with p_RA2I / p_I2RA
+ * (:707-719), and write_different_training_arrangements (:406-457).  Draws come from the
+ * (seed, stream_id) topology streams, so a topology is a function of its arguments. */
+typedef enum { UG_ARRANGEMENT_SPHERE = 0, UG_ARRANGEMENT_SQUARE = 1 } ug_arrangement;
+
+/* TopologyParameters, c++/include/ConfigurationNetworkTopology.h:11-22 */
+typedef struct {
+    int32_t arrangement;   /* ug_arrangement */
+    int32_t _pad;
+    double A_RA2I, SIGMA_RA2I, B_I2RA, SIGMA_I2RA;
+} ug_topology_params;
+
+typedef struct ug_topology ug_topology;
+
+typedef struct {
+    int32_t n_ra, n_i, n_tr, dim;   /* dim: 3 on the sphere, 2 on the square */
+    int64_t n_ra2i, n_i2ra;         /* connections in each direction */
+    int64_t ra_attempts;            /* HVC(RA) placement attempts drawn */
+    int64_t i_retries;              /* interneuron placements drawn again */
+    double model_distance;          /* MODEL_INTERNEURON_DISTANCE */
+    double device_ms;               /* device time of the generation, and of its three stages: */
+    double interneuron_ms, placement_ms, connection_ms;
+    int64_t launches;               /* kernels it launched */
+    int32_t batches;                /* HVC(RA) placement batches */
+    int32_t _pad;
+} ug_topology_info;
+
+/* Samples a topology on the context's device; *out is freed with ug_topology_free.
+ * UG_EINVAL for bad sizes or when the minimum-distance rejection sampling gives up. */
+ug_status ug_generate_topology(ug_ctx* ctx, const ug_topology_params* params, int32_t n_ra, int32_t n_i,
+                               int32_t n_tr, uint64_t seed, int32_t stream_id, ug_topology** out);
+ug_status ug_topology_get_info(const ug_topology* t, ug_topology_info* info);
+/* Coordinates, 3 per neuron (z = 0 on the square): ra_xyz [n_ra][3], i_xyz [n_i][3]. */
+ug_status ug_topology_get_coordinates(const ug_topology* t, double* ra_xyz, double* i_xyz);
+/* which 0: RA->I (offsets [n_ra+1]), 1: I->RA (offsets [n_i+1]); targets and lengths
+ * (microns) [n_ra2i or n_i2ra], in the reference's order (by source, then target). */
+ug_status ug_topology_get_connections(const ug_topology* t, int32_t which, int32_t* offsets, int32_t* targets,
+                                      double* lengths);
+/* which 0: training_neurons_clustered, 1: training_neurons_random; [n_tr]. */
+ug_status ug_topology_get_training(const ug_topology* t, int32_t which, int32_t* neurons);
+/* write_network_topology (:18294-18310), write_pajek_topology (:18367-18429) and the two
+ * training files into `network_dir`. */
+ug_status ug_topology_write_dir(const ug_topology* t, const char* network_dir);
+void ug_topology_free(ug_topology* t);
+/* createNetworkForGrowth (c++/createNetworkForGrowth/main.cpp): reads the spatialParameters
+ * of `config_file` and writes a generated topology into `network_dir`. */
+ug_status ug_create_network_topology(ug_ctx* ctx, const char* config_file, const char* network_dir, int32_t n_ra,
+                                     int32_t n_i, int32_t n_tr, uint64_t seed, ug_topology_info* info);
+
 /* No counterpart in the reference (measurement support): measured throughput of the
  * SFU (ex2/rcp approximations, operations per second) and of FP32 FMA on `device`,
  * the denominators of the integrators' roofline. */

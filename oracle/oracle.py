@@ -154,6 +154,51 @@ def philox(ctr, key):
     return list(o)
 
 
+class TopologyParams(C.Structure):
+    _fields_ = [("arrangement", C.c_int32), ("_pad", C.c_int32)] + [
+        (n, C.c_double) for n in ("A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA")]
+
+
+ARRANGEMENTS = {"sphere": 0, "square": 1}
+
+
+def topology_model_distance(arrangement: str, n_i: int) -> float:
+    L = lib()
+    L.ugo_topology_model_distance.restype = C.c_double
+    L.ugo_topology_model_distance.argtypes = [C.c_int32, C.c_int32]
+    return L.ugo_topology_model_distance(ARRANGEMENTS[arrangement], n_i)
+
+
+def generate_topology(params: dict, n_ra: int, n_i: int, n_tr: int, seed: int, net: int = 0,
+                      arrangement: str = "sphere", max_misses: int = 1 << 16) -> dict:
+    """The sequential restatement of createNetworkForGrowth's sampling
+    (ugo_topology.cpp): coordinates, RA->I / I->RA CSR lists with lengths,
+    the clustered and random training sets and the attempt counters."""
+    L = lib()
+    f = L.ugo_generate_topology
+    f.restype = C.c_int
+    f.argtypes = [_P(TopologyParams), C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.c_uint32, C.c_int64,
+                  _f64p, _f64p, _f64p, _i32p, _i32p, _f64p, C.c_int64, _i32p, _i32p, _f64p, C.c_int64,
+                  _i32p, _i32p, _P(C.c_int64)]
+    p = TopologyParams(ARRANGEMENTS[arrangement], 0, *(float(params[k]) for k in
+                                                       ("A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA")))
+    cap = n_ra * n_i
+    ra, ii, model = np.zeros((n_ra, 3)), np.zeros((n_i, 3)), C.c_double()
+    ri_off, ir_off = np.zeros(n_ra + 1, dtype=np.int32), np.zeros(n_i + 1, dtype=np.int32)
+    ri_tgt, ir_tgt = np.zeros(max(cap, 1), dtype=np.int32), np.zeros(max(cap, 1), dtype=np.int32)
+    ri_len, ir_len = np.zeros(max(cap, 1)), np.zeros(max(cap, 1))
+    cl, rn = np.zeros(max(n_tr, 1), dtype=np.int32), np.zeros(max(n_tr, 1), dtype=np.int32)
+    counters = (C.c_int64 * 2)()
+    rc = f(C.byref(p), n_ra, n_i, n_tr, seed, net, max_misses, _ptr(ra, _f64p), _ptr(ii, _f64p), C.byref(model),
+           _ptr(ri_off, _i32p), _ptr(ri_tgt, _i32p), _ptr(ri_len, _f64p), cap, _ptr(ir_off, _i32p),
+           _ptr(ir_tgt, _i32p), _ptr(ir_len, _f64p), cap, _ptr(cl, _i32p), _ptr(rn, _i32p), counters)
+    if rc != 0:
+        raise RuntimeError(f"ugo_generate_topology failed ({rc})")
+    return dict(ra_xyz=ra, i_xyz=ii, model=model.value, ri=(ri_off, ri_tgt[:ri_off[-1]], ri_len[:ri_off[-1]]),
+                ir=(ir_off, ir_tgt[:ir_off[-1]], ir_len[:ir_off[-1]]), clustered=cl[:n_tr], random=rn[:n_tr],
+                ra_attempts=counters[0], i_retries=counters[1])
+
+
 def _kicks(kicks):
     kicks = sorted(kicks or [])
     steps = np.array([k[0] for k in kicks], dtype=np.int32)

@@ -133,6 +133,21 @@ void ugo_i_single(int32_t n_steps, uint64_t seed, uint32_t trial, uint32_t neuro
                   int32_t n_kicks, double* trace_out, uint8_t* fired_out);
 void ugo_philox(const uint32_t* ctr, const uint32_t* key, uint32_t* out);
 
+/* Network topology generation (ugo_topology.cpp).  arrangement 0 = sphere, 1 = square. */
+typedef struct {
+    int32_t arrangement;
+    int32_t _pad;
+    double A_RA2I, SIGMA_RA2I, B_I2RA, SIGMA_I2RA;
+} ugo_topology_params;
+double ugo_topology_model_distance(int32_t arrangement, int32_t n_i);
+/* 0 on success; -1 one neuron was rejected more than max_misses times in a row; -2 an edge buffer is full;
+ * -3 bad sizes.  counters[0] = HVC(RA) attempts made, counters[1] = interneuron re-tries. */
+int ugo_generate_topology(const ugo_topology_params* p, int32_t n_ra, int32_t n_i, int32_t n_tr, uint64_t seed,
+                          uint32_t net, int64_t max_misses, double* ra_xyz, double* i_xyz, double* model_out,
+                          int32_t* ri_off, int32_t* ri_tgt, double* ri_len, int64_t ri_cap, int32_t* ir_off,
+                          int32_t* ir_tgt, double* ir_len, int64_t ir_cap, int32_t* clustered, int32_t* random_tr,
+                          int64_t* counters);
+
 #ifdef __cplusplus
 }
 #endif

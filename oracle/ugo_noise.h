@@ -33,7 +33,8 @@ enum {
     UGO_KIND_RA_WHITE = 1,    /* HVC(RA) white-noise point distribution, 4 words per step */
     UGO_KIND_I_POISSON = 2,   /* HVC(I) Poisson conductance noise, sequential words */
     UGO_KIND_TRIAL = 3,       /* per-trial network draws (mean injection time) */
-    UGO_KIND_REPLACE = 4      /* neuron replacement resampling */
+    UGO_KIND_REPLACE = 4,     /* neuron replacement resampling */
+    UGO_KIND_TOPOLOGY = 6     /* network topology generation (coordinates, RA<->I connections) */
 };
 
 static inline uint32_t ugo_mulhilo32(uint32_t a, uint32_t b, uint32_t* hi)

@@ -1,9 +1,11 @@
 """Builds the CUDA trial engine, libugrowth.so, in-tree for sm_103a.
 
-nvcc compiles the three translation units in parallel: the double-precision
+nvcc compiles the translation units in parallel: the double-precision
 kernels (without multiply-add contraction, so they keep the reference's
-rounding sequence), the single-precision kernels, and the host side with the
-C ABI of include/ugrowth.h.
+rounding sequence), the single-precision kernels, the host side with the
+C ABI of include/ugrowth.h, the pipe calibration, the reference's file
+formats, and the topology generator (also without contraction); then the
+command-line programs.
 """
 from __future__ import annotations
 
@@ -25,7 +27,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I" + CSRC, "-I" + os.path.join(ROOT, "include")]
 CLI_SRC = "ug_cli.cpp"
 UNITS = [("ug_kernels_f64.cu", ["-fmad=false"]), ("ug_kernels_f32.cu", []), ("ug_host.cu", []), ("ug_calib.cu", []),
-         ("ug_files.cpp", [])]
+         ("ug_files.cpp", []), ("ug_topology.cu", ["-fmad=false"])]
 
 
 def nvcc() -> str:

@@ -1,7 +1,8 @@
-// ug_growth: the reference's three simulation programs on the GB300 engine, with
-// their argument lists (c++/chainGrowth/main.cpp, c++/continueChainGrowth/main.cpp,
-// c++/chainTest/main.cpp) and their output files.
+// ug_growth: the reference's four programs on the GB300 engine, with their argument
+// lists (c++/createNetworkForGrowth/main.cpp, c++/chainGrowth/main.cpp,
+// c++/continueChainGrowth/main.cpp, c++/chainTest/main.cpp) and their output files.
 //
+//   ug_growth createNetworkForGrowth <topology config> <network dir>
 //   ug_growth chainGrowth <network dir> <training neurons file> <growth config> <output dir>
 //   ug_growth continueChainGrowth <data dir> <output dir> <starting trial>
 //   ug_growth chainTest <network dir> <trial number> <number of test trials> <output dir>
@@ -10,7 +11,9 @@
 // reference runs until stopped), --save-short K, --save-long K (the reference's
 // save frequencies: 75/150 for chainGrowth, 50/100 for continueChainGrowth),
 // --precision 32|64, --device D, --seed S (noise streams; 15000 by default),
-// --spike-capacity C (spikes recorded per neuron and trial for the spike files).
+// --spike-capacity C (spikes recorded per neuron and trial for the spike files);
+// createNetworkForGrowth takes --n-ra, --n-i, --n-tr (2000, 550 and 10, the sizes its
+// reference main hard-codes), --seed and --device.
 //
 // Growth saves are written after a trial's between-trial bookkeeping, so
 // continueChainGrowth from a saved trial T runs trials T + 1, T + 2, ...
@@ -27,6 +30,7 @@ namespace {
 struct Opts {
     long trials = -1;
     int save_short = -1, save_long = -1, precision = 32, device = 0, spikes = 256;
+    int n_ra = 2000, n_i = 550, n_tr = 10;
     unsigned long long seed = 15000;
 };
 
@@ -46,6 +50,9 @@ bool parse_opts(int argc, char** argv, int first, Opts& o)
         else if (a == "--device") o.device = std::atoi(v);
         else if (a == "--seed") o.seed = std::strtoull(v, nullptr, 10);
         else if (a == "--spike-capacity") o.spikes = std::atoi(v);
+        else if (a == "--n-ra") o.n_ra = std::atoi(v);
+        else if (a == "--n-i") o.n_i = std::atoi(v);
+        else if (a == "--n-tr") o.n_tr = std::atoi(v);
         else {
             std::fprintf(stderr, "unknown option %s\n", a.c_str());
             return false;
@@ -93,6 +100,7 @@ int usage()
 {
     std::fprintf(stderr,
                  "usage:\n"
+                 "  ug_growth createNetworkForGrowth <topology config> <network dir> [--n-ra N --n-i N --n-tr N]\n"
                  "  ug_growth chainGrowth <network dir> <training neurons file> <growth config> <output dir> [options]\n"
                  "  ug_growth continueChainGrowth <data dir> <output dir> <starting trial> [options]\n"
                  "  ug_growth chainTest <network dir> <trial number> <number of test trials> <output dir> [options]\n"
@@ -107,7 +115,11 @@ int main(int argc, char** argv)
 {
     if (argc < 2) return usage();
     const std::string cmd = argv[1];
-    const int npos = cmd == "chainGrowth" ? 4 : cmd == "continueChainGrowth" ? 3 : cmd == "chainTest" ? 4 : -1;
+    const int npos = cmd == "chainGrowth"              ? 4
+                     : cmd == "continueChainGrowth"    ? 3
+                     : cmd == "chainTest"              ? 4
+                     : cmd == "createNetworkForGrowth" ? 2
+                                                       : -1;
     if (npos < 0 || argc < 2 + npos) return usage();
     Opts o;
     if (cmd == "continueChainGrowth") {
@@ -124,7 +136,15 @@ int main(int argc, char** argv)
     if (check(ug_create(&ctx, &ro), "ug_create")) return 1;
     int rc = 0;
     int32_t net = -1;
-    if (cmd == "chainGrowth") {
+    if (cmd == "createNetworkForGrowth") {
+        // generate_network_topology (NetworkGrowthSimulator.cpp:110-155)
+        ug_topology_info info;
+        rc = check(ug_create_network_topology(ctx, argv[2], argv[3], o.n_ra, o.n_i, o.n_tr, o.seed, &info),
+                   "generate_network_topology");
+        if (!rc)
+            std::printf("Model interneuron distance = %g\nN_RA = %d, N_I = %d: %lld RA->I and %lld I->RA connections\n",
+                        info.model_distance, info.n_ra, info.n_i, (long long)info.n_ra2i, (long long)info.n_i2ra);
+    } else if (cmd == "chainGrowth") {
         const std::string out = argv[5];
         rc = check(ug_create_growth_network(ctx, argv[2], argv[3], argv[4], out.c_str(), 0, o.seed, 0, &net),
                    "network set-up");

@@ -8,6 +8,7 @@
 // (groups of scalar settings, '=' or ':', quoted strings, comments).
 #include "ugrowth.h"
 #include "ug_philox.cuh"
+#include "ug_topology.h"
 
 #include <algorithm>
 #include <cctype>
@@ -20,7 +21,6 @@
 #include <string>
 #include <vector>
 
-void ug_set_last_error(const std::string& msg);   // ug_host.cu
 
 namespace {
 
@@ -259,12 +259,17 @@ void write_connections(Out& o, int n, const std::vector<int32_t>& off, const std
     }
 }
 
-void write_coords(Out& o, int n, const std::vector<double>& xyz, double model)
+// write_coordinates (:18431-18500): 3 coordinates per neuron on the sphere, x and y on the square
+void write_coords(Out& o, int n, const std::vector<double>& xyz, double model, int dim = 3)
 {
     o.put((int32_t)n);
-    o.put((int32_t)3);
+    o.put((int32_t)dim);
     o.put(model);
-    o.put(xyz.data(), xyz.size());
+    if (dim == 3) {
+        o.put(xyz.data(), xyz.size());
+        return;
+    }
+    for (int i = 0; i < n; ++i) o.put(&xyz[3 * (size_t)i], (size_t)dim);
 }
 
 ug_status closed(Out& o, const std::string& path)
@@ -970,4 +975,112 @@ extern "C" ug_status ug_create_growth_network(ug_ctx* ctx, const char* network_d
     d.training = training.data(); d.training_spread = spread.data();
     d.ra_xyz = ra_xyz.data(); d.i_xyz = i_xyz.data();
     return ug_load_network(ctx, &d, net_id);
+}
+
+// ---------------------------------------------------------------- generated topologies
+
+namespace {
+
+// std::ostream's default rendering of a double (six significant digits)
+std::string g6(double v)
+{
+    char b[64];
+    std::snprintf(b, sizeof(b), "%g", v);
+    return b;
+}
+
+}  // namespace
+
+extern "C" ug_status ug_topology_write_dir(const ug_topology* t, const char* dir_c)
+{
+    if (!t || !dir_c) return ferr(UG_EINVAL, "null argument");
+    const std::string dir(dir_c);
+    const int dim = t->dim();
+    // write_network_topology (:18294-18310)
+    const std::string pi = join(dir, "I_xy.bin"), pr = join(dir, "RA_xy.bin");
+    Out oi(pi, false), orr(pr, false);
+    write_coords(oi, t->n_i, t->i_xyz, t->model, dim);
+    write_coords(orr, t->n_ra, t->ra_xyz, t->model, dim);
+    UG_FTRY(closed(oi, pi));
+    UG_FTRY(closed(orr, pr));
+    // write_connections_RAandI (:18312-18365): weights sample_G(0.0) = 0, delays 0
+    const std::string p1 = join(dir, "RA_I_connections.bin"), p2 = join(dir, "I_RA_connections.bin");
+    Out a(p1, false), b(p2, false);
+    const std::vector<double> zri(t->ri_tgt.size(), 0.0), zir(t->ir_tgt.size(), 0.0);
+    write_connections(a, t->n_ra, t->ri_off, t->ri_tgt, zri, t->ri_len, zri);
+    write_connections(b, t->n_i, t->ir_off, t->ir_tgt, zir, t->ir_len, zir);
+    UG_FTRY(closed(a, p1));
+    UG_FTRY(closed(b, p2));
+    const std::string pn = join(dir, "num_neurons.bin");
+    Out on(pn, false);
+    on.put((int32_t)t->n_ra);
+    on.put((int32_t)t->n_i);
+    UG_FTRY(closed(on, pn));
+    // write_different_training_arrangements (:406-457)
+    for (int which = 0; which < 2; ++which) {
+        const std::string p = join(dir, which == 0 ? "training_neurons_clustered.bin" : "training_neurons_random.bin");
+        const std::vector<int32_t>& v = which == 0 ? t->clustered : t->random_set;
+        Out o(p, false);
+        o.put((int32_t)v.size());
+        o.put(v.data(), v.size());
+        UG_FTRY(closed(o, p));
+    }
+    // write_pajek_topology (:18367-18429); the training neurons it marks are the random set,
+    // the last one generate_network_topology assigned
+    std::vector<char> training(t->n_ra, 0);
+    for (int32_t id : t->random_set) training[id] = 1;
+    std::string s = "*Vertices " + std::to_string(t->n_ra + t->n_i) + "\n";
+    auto coords = [&](const std::vector<double>& xyz, int i) {
+        std::string c = g6(xyz[3 * (size_t)i]) + " " + g6(xyz[3 * (size_t)i + 1]);
+        if (dim == 3) c += " " + g6(xyz[3 * (size_t)i + 2]);
+        return c;
+    };
+    for (int i = 0; i < t->n_ra; ++i)
+        s += std::to_string(i + 1) + " \"" + std::to_string(i) + "\" " + coords(t->ra_xyz, i) +
+             (training[i] ? " ic Yellow\n" : " ic Green\n");
+    for (int i = 0; i < t->n_i; ++i)
+        s += std::to_string(i + t->n_ra + 1) + " \"" + std::to_string(i + t->n_ra) + "\" " + coords(t->i_xyz, i) +
+             " ic Red\n";
+    s += "*Arcs\n";
+    for (int i = 0; i < t->n_ra; ++i)
+        for (int32_t k = t->ri_off[i]; k < t->ri_off[i + 1]; ++k)
+            s += std::to_string(i + 1) + " " + std::to_string(t->ri_tgt[k] + t->n_ra + 1) + " " + g6(0.0) + " c Green\n";
+    for (int i = 0; i < t->n_i; ++i)
+        for (int32_t k = t->ir_off[i]; k < t->ir_off[i + 1]; ++k)
+            s += std::to_string(i + t->n_ra + 1) + " " + std::to_string(t->ir_tgt[k] + 1) + " " + g6(0.0) + " c Red\n";
+    const std::string pp = join(dir, "network_topology.net");
+    std::ofstream f(pp);
+    f << s;
+    f.close();
+    return f ? UG_OK : ferr(UG_EIO, "cannot write " + pp);
+}
+
+extern "C" ug_status ug_create_network_topology(ug_ctx* ctx, const char* config_file, const char* network_dir,
+                                                int32_t n_ra, int32_t n_i, int32_t n_tr, uint64_t seed,
+                                                ug_topology_info* info)
+{
+    if (!ctx || !config_file || !network_dir) return ferr(UG_EINVAL, "null argument");
+    Cfg c;
+    UG_FTRY(parse_cfg(config_file, c));
+    ug_topology_params p;
+    std::memset(&p, 0, sizeof(p));
+    std::string arrangement;
+    auto gi = c.groups.find("spatialParameters");
+    if (gi != c.groups.end() && gi->second.count("arrangement")) arrangement = gi->second.at("arrangement");
+    if (arrangement == "sphere")
+        p.arrangement = UG_ARRANGEMENT_SPHERE;
+    else if (arrangement == "square")
+        p.arrangement = UG_ARRANGEMENT_SQUARE;
+    else
+        return ferr(UG_EINVAL, "arrangement \"" + arrangement + "\" is not generated (sphere or square)");
+    c.num("spatialParameters", "A_RA2I", p.A_RA2I);
+    c.num("spatialParameters", "SIGMA_RA2I", p.SIGMA_RA2I);
+    c.num("spatialParameters", "B_I2RA", p.B_I2RA);
+    c.num("spatialParameters", "SIGMA_I2RA", p.SIGMA_I2RA);
+    ug_topology* t = nullptr;
+    UG_FTRY(ug_generate_topology(ctx, &p, n_ra, n_i, n_tr, seed, 0, &t));
+    const ug_status s = ug_topology_write_dir(t, network_dir);
+    if (s == UG_OK && info) ug_topology_get_info(t, info);
+    ug_topology_free(t);
+    return s;
 }

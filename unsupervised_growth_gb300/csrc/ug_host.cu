@@ -2203,6 +2203,12 @@ ug_status ug_launch_count(ug_ctx* ctx, int64_t* out)
 
 }  // extern "C"
 
+// A context as the other translation units see it (the topology generator).
+int ug_ctx_device(ug_ctx* ctx) { return ctx->device; }
+cudaStream_t ug_ctx_stream(ug_ctx* ctx) { return ctx->stream; }
+std::recursive_mutex& ug_ctx_mutex(ug_ctx* ctx) { return ctx->mu; }
+void ug_ctx_add_launches(ug_ctx* ctx, int64_t n) { ctx->launches += n; }
+
 // ------------------------------------------------------------------------
 // Test trial without device allocation.
 //

@@ -28,7 +28,8 @@ enum NoiseKind : uint32_t {
     kNoiseIPoisson = 2,   // HVC(I) Poisson conductance noise: sequential words
     kNoiseTrial = 3,      // per-trial network draws (mean training injection time)
     kNoiseReplace = 4,    // neuron replacement resampling
-    kNoiseCreate = 5      // network set-up draws (the growth CLI's weight resampling)
+    kNoiseCreate = 5,     // network set-up draws (the growth CLI's weight resampling)
+    kNoiseTopology = 6    // topology generation: coordinates and RA<->I connections
 };
 
 struct Philox4 { uint32_t x, y, z, w; };

@@ -31,7 +31,9 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_append_num_synapses", "ug_append_replaced", "ug_write_jitter", "ug_write_spike_times",
             "ug_write_graph_state", "ug_create_growth_network", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
-            "ug_run_test_trial_noalloc", "ug_calibrate_pipes"]
+            "ug_run_test_trial_noalloc", "ug_generate_topology", "ug_topology_get_info",
+            "ug_topology_get_coordinates", "ug_topology_get_connections", "ug_topology_get_training",
+            "ug_topology_write_dir", "ug_topology_free", "ug_create_network_topology", "ug_calibrate_pipes"]
 
 
 class UGError(RuntimeError):
@@ -65,6 +67,10 @@ class ConnectionParams(C.Structure):
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
+
+
+def _ptr(a: np.ndarray, t):
+    return a.ctypes.data_as(t)
 
 
 class NetworkDesc(C.Structure):
@@ -111,6 +117,21 @@ class RequestInfo(C.Structure):
                 ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
                 ("footprint_bytes", C.c_int64), ("error", C.c_char * 256)]
 
+
+class TopologyParams(C.Structure):
+    _fields_ = [("arrangement", C.c_int32), ("_pad", C.c_int32)] + [
+        (n, C.c_double) for n in ("A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA")]
+
+
+class TopologyInfo(C.Structure):
+    _fields_ = [("n_ra", C.c_int32), ("n_i", C.c_int32), ("n_tr", C.c_int32), ("dim", C.c_int32),
+                ("n_ra2i", C.c_int64), ("n_i2ra", C.c_int64), ("ra_attempts", C.c_int64), ("i_retries", C.c_int64),
+                ("model_distance", C.c_double), ("device_ms", C.c_double), ("interneuron_ms", C.c_double),
+                ("placement_ms", C.c_double), ("connection_ms", C.c_double), ("launches", C.c_int64),
+                ("batches", C.c_int32), ("_pad", C.c_int32)]
+
+
+ARRANGEMENTS = {"sphere": 0, "square": 1}
 
 REQUEST_STATE = {0: "queued", 1: "running", 2: "done", 3: "failed"}
 
@@ -172,8 +193,19 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_kernel_timing.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.ug_run_test_trial_noalloc.argtypes = [vp, C.c_int32, C.c_uint32] + [C.c_void_p] * 6
     L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ug_generate_topology.argtypes = [vp, C.POINTER(TopologyParams), C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                       C.c_int32, C.POINTER(vp)]
+    L.ug_topology_get_info.argtypes = [vp, C.POINTER(TopologyInfo)]
+    L.ug_topology_get_coordinates.argtypes = [vp, _f64p, _f64p]
+    L.ug_topology_get_connections.argtypes = [vp, C.c_int32, _i32p, _i32p, _f64p]
+    L.ug_topology_get_training.argtypes = [vp, C.c_int32, _i32p]
+    L.ug_topology_write_dir.argtypes = [vp, C.c_char_p]
+    L.ug_topology_free.argtypes = [vp]
+    L.ug_topology_free.restype = None
+    L.ug_create_network_topology.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
+                                             C.POINTER(TopologyInfo)]
     for name in EXPORTED:
-        if name not in ("ug_last_error", "ug_destroy"):
+        if name not in ("ug_last_error", "ug_destroy", "ug_topology_free"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -431,11 +463,75 @@ class Engine:
         net = Network(n_ra=x.n_ra, n_i=x.n_i, seed=seed, num_steps=x.num_steps, net_id=stream_id)
         return ResidentNetwork(self, net, nid.value)
 
+    def generate_topology(self, params: dict, n_ra: int, n_i: int, n_tr: int = 10, seed: int = 15000,
+                          stream_id: int = 0, arrangement: str = "sphere") -> "Topology":
+        """generate_network_topology on the device (coordinates, RA<->I connections and the
+        two training arrangements); params holds A_RA2I, SIGMA_RA2I, B_I2RA, SIGMA_I2RA."""
+        p = TopologyParams(ARRANGEMENTS[arrangement], 0,
+                           *(float(params[k]) for k in ("A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA")))
+        h = C.c_void_p()
+        _check(self.L.ug_generate_topology(self.ctx, C.byref(p), n_ra, n_i, n_tr, seed, stream_id, C.byref(h)))
+        return Topology(self.L, h)
+
+    def create_network_topology(self, config_file: str, network_dir: str, n_ra: int = 2000, n_i: int = 550,
+                                n_tr: int = 10, seed: int = 15000) -> dict:
+        """createNetworkForGrowth: a generated topology written into network_dir."""
+        x = TopologyInfo()
+        _check(self.L.ug_create_network_topology(self.ctx, config_file.encode(), network_dir.encode(), n_ra, n_i,
+                                                 n_tr, seed, C.byref(x)))
+        return {k: getattr(x, k) for k, _ in TopologyInfo._fields_}
+
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
         nid = C.c_int32(-1)
         _check(self.L.ug_load_network(self.ctx, C.byref(d), C.byref(nid)))
         return ResidentNetwork(self, net, nid.value)
+
+
+class Topology:
+    """A generated topology held by the library (ug_topology); arrays are copied out."""
+
+    def __init__(self, L, handle):
+        self.L, self.h = L, handle
+        x = TopologyInfo()
+        _check(L.ug_topology_get_info(self.h, C.byref(x)))
+        self.info = {k: getattr(x, k) for k, _ in TopologyInfo._fields_}
+        self.n_ra, self.n_i, self.n_tr = x.n_ra, x.n_i, x.n_tr
+        self.model = x.model_distance
+
+    def coordinates(self):
+        ra, ii = np.zeros((self.n_ra, 3)), np.zeros((self.n_i, 3))
+        _check(self.L.ug_topology_get_coordinates(self.h, _ptr(ra, _f64p), _ptr(ii, _f64p)))
+        return ra, ii
+
+    def connections(self, which: int):
+        """(offsets, targets, lengths) of RA->I (0) or I->RA (1)."""
+        n_src = self.n_ra if which == 0 else self.n_i
+        n = self.info["n_ra2i"] if which == 0 else self.info["n_i2ra"]
+        off = np.zeros(n_src + 1, dtype=np.int32)
+        tgt, ln = np.zeros(max(n, 1), dtype=np.int32), np.zeros(max(n, 1))
+        _check(self.L.ug_topology_get_connections(self.h, which, _ptr(off, _i32p), _ptr(tgt, _i32p), _ptr(ln, _f64p)))
+        return off, tgt[:n], ln[:n]
+
+    def training(self, which: int):
+        """training_neurons_clustered (0) or training_neurons_random (1)."""
+        out = np.zeros(max(self.n_tr, 1), dtype=np.int32)
+        _check(self.L.ug_topology_get_training(self.h, which, _ptr(out, _i32p)))
+        return out[:self.n_tr]
+
+    def write_dir(self, directory: str):
+        _check(self.L.ug_topology_write_dir(self.h, directory.encode()))
+
+    def free(self):
+        if self.h:
+            self.L.ug_topology_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def calibrate_pipes(device: int = 0):
