@@ -487,6 +487,64 @@ def run_uneven(args, local_rank):
     return res
 
 
+def run_create(args, local_rank):
+    """createNetworkForGrowth on the device: a step generates one network topology
+    (coordinates with minimum-distance rejection, RA<->I connections, training
+    arrangements) of the given size on the sphere, each step from its own seed.
+    value: networks/s of device time; e2e: networks/s through ug_generate_topology
+    (host arrays out, device-to-host copies included); cpu_baseline: the sequential
+    oracle on one core, a few networks of the same size."""
+    import math
+
+    import torch
+
+    from oracle import oracle as O
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    B.build()
+    torch.cuda.set_device(local_rank)
+    n_ra, n_i = (int(x) for x in args.create_size.split("x"))
+    p = dict(A_RA2I=0.1, SIGMA_RA2I=120 / math.sqrt(2.0), B_I2RA=0.1, SIGMA_I2RA=120 / math.sqrt(2.0))
+    eng = Engine(precision=32, device=local_rank)
+    for s in range(args.warmup):
+        eng.generate_topology(p, n_ra, n_i, 10, seed=1000 + s).free()
+    dev_ms, walls, edges, launches, stages = [], [], 0, 0, [0.0, 0.0, 0.0]
+    d2h = 0
+    with ClockSampler(local_rank) as clk:
+        for s in range(args.steps):
+            t0 = time.perf_counter()
+            t = eng.generate_topology(p, n_ra, n_i, 10, seed=s)
+            walls.append(time.perf_counter() - t0)
+            i = t.info
+            dev_ms.append(i["device_ms"])
+            edges += i["n_ra2i"] + i["n_i2ra"]
+            launches += i["launches"]
+            stages = [a + b for a, b in zip(stages, (i["interneuron_ms"], i["placement_ms"], i["connection_ms"]))]
+            d2h = 24 * (n_ra + n_i) + 4 * (n_ra + n_i + 2) + 12 * (i["n_ra2i"] + i["n_i2ra"])
+            t.free()
+    value = 1e3 * args.steps / sum(dev_ms)
+    e2e = args.steps / sum(walls)
+    # the oracle on one core, a bounded sample
+    ncpu = max(1, min(args.steps, 5 if n_ra <= 4000 else 1))
+    t0 = time.perf_counter()
+    for s in range(ncpu):
+        O.generate_topology(p, n_ra, n_i, 10, seed=s)
+    cpu = ncpu / (time.perf_counter() - t0)
+    return {"metric": f"networks/s (createNetworkForGrowth topology, {n_ra} RA + {n_i} I on the sphere)",
+            "value": value, "unit": "networks/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sum(dev_ms) / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (f32 prefilters)", "data": "synthetic (seeded topology streams)",
+            "config": {"workload": f"topology generation, {n_ra} HVC-RA + {n_i} HVC-I on the sphere, A = 0.1, "
+                                   f"sigma = 120/sqrt(2) um, 10 training neurons, a new seed per step",
+                       "stage_ms": {"interneurons": stages[0] / args.steps, "placement": stages[1] / args.steps,
+                                    "connections": stages[2] / args.steps},
+                       "edges_per_network": edges / args.steps, "l2": "inputs are a few MB; not flushed"},
+            "e2e": {"value": e2e, "unit": "networks/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "cpu_baseline": {"value": cpu, "unit": "networks/s", "cores": 1, "kind": "port",
+                             "sample": f"{ncpu} networks of the same size from the sequential oracle"}}
+
+
 def run_serve(args, local_rank):
     """Serving: growth and test-trial requests of mixed network size arrive as a
     Poisson stream; the engine's scheduler admits them by device footprint into the
@@ -658,11 +716,13 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="test", choices=["test", "growth", "uneven", "serve", "topology"],
+    ap.add_argument("--workload", default="test",
+                    choices=["test", "growth", "uneven", "serve", "topology", "create"],
                     help="test: batched test trials (the headline); growth: consecutive growth trials of one "
                          "network; uneven: one group of growing networks of uneven size; serve: a Poisson stream "
                          "of requests through the serving loop; topology: single vs double precision over "
-                         "consecutive growth trials")
+                         "consecutive growth trials; create: network topology generation (createNetworkForGrowth)")
+    ap.add_argument("--create-size", default="2000x550", help="create: HVC(RA) x HVC(I)")
     ap.add_argument("--members", type=int, default=64, help="uneven: networks in the group; serve: member slots")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")
@@ -687,6 +747,8 @@ def main():
         res = run_serve(args, local_rank) if rank == 0 else None
     elif args.workload == "topology":
         res = run_topology(args, local_rank) if rank == 0 else None
+    elif args.workload == "create":
+        res = run_create(args, local_rank) if rank == 0 else None
     else:
         res = run_ours(args, rank, world, local_rank)
     if rank == 0 and res is not None:

@@ -7,9 +7,10 @@
 // draw has its own place in the topology streams (kind kNoiseTopology; the trial field
 // names the purpose), so the sequential loops become parallel ones with the same result:
 //
-// * Interneurons (one block).  Interneuron i's r-th try uses words 2r, 2r+1 of stream i.
-//   Every pending interneuron's current try is checked against all earlier ones at once;
-//   the first that is too close draws again until it fits, and the check resumes after it.
+// * Interneurons.  Interneuron i's r-th try uses words 2r, 2r+1 of stream i.  Every first
+//   try is checked against all earlier ones at once (a warp per interneuron over the grid);
+//   from the first that is too close on, one block lets it draw again until it fits and
+//   then searches the next conflict among the later ones, until there is none.
 // * HVC(RA) placement.  The a-th attempt uses stream entity a, so the reference's loop
 //   (attempt until far enough from every interneuron and every earlier HVC(RA)) keeps
 //   exactly the attempts that are far enough from every interneuron and every attempt
@@ -44,7 +45,7 @@ constexpr double kExpDist = 40.0;   // EXPERIMENTAL_INTERNEURON_DISTANCE (Networ
 constexpr double kMinDist = 10.0;   // MIN_INTERSOMATIC_DISTANCE (:20)
 constexpr double kShift = 0.15;     // interneuron jitter in model spacings (sample_coordinates :224)
 constexpr int kMaxPartners = 16;    // conflicts one attempt may have inside its batch
-constexpr int kMaxBatch = 4096;
+constexpr int kMaxBatch = 16384;
 constexpr int kMinBatch = 64;
 constexpr int kResolveThreads = 1024;
 constexpr int kChunk = 256;         // points staged in shared memory per block
@@ -72,6 +73,7 @@ struct State {
     int count;            // HVC(RA) placed
     int overflow;         // a batch attempt had more than kMaxPartners conflicts
     int status;           // 1: an interneuron found no place
+    int first;            // the first interneuron whose first try is too close to an earlier one
     int kept;             // attempts kept by the last batch (before the cut at N_RA)
     int unflagged;        // attempts of the last batch far enough from the points placed before it
     long long attempts;   // attempts consumed
@@ -176,63 +178,56 @@ __device__ void i_try(const Geo& g, int i, uint32_t r, double z, double phi, dou
     t[2] = cos(theta + theta_noise);
 }
 
-__global__ void __launch_bounds__(1024) k_interneurons(Geo g, int n_i, double* xyz, float4* xyz32, double* base,
+// every interneuron's first try on the sphere, at its point of the Fibonacci lattice
+// (base: z and phi as :296-300 accumulate them); the square grid (:231-241), whose side^2
+// jittered points are final and whose remaining interneurons stay at the origin
+__global__ void k_i_first_tries(Geo g, int n_i, const double* base, double* xyz, float4* xyz32, State* st)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q == 0) st->first = n_i;
+    if (q >= n_i) return;
+    if (g.sphere) {
+        i_try(g, q, 0, base[2 * q], base[2 * q + 1], xyz + 3 * q);
+    } else if (q < g.side * g.side) {
+        const int i = q / g.side, k = q % g.side;
+        const ug::Philox4 b =
+            ug::stream_block(ug::make_stream(g.seed, ug::kNoiseTopology, g.net, (uint32_t)q, kPartInterneuron), 0);
+        xyz[3 * q] = (double)(i + 1) / (g.root + 1) - kShift * g.model + ug::random_G(2 * kShift * g.model, b.x);
+        xyz[3 * q + 1] = (double)(k + 1) / (g.root + 1) - kShift * g.model + ug::random_G(2 * kShift * g.model, b.y);
+        xyz[3 * q + 2] = 0.0;
+    } else {
+        xyz[3 * q] = xyz[3 * q + 1] = xyz[3 * q + 2] = 0.0;
+    }
+    xyz32[q] = to32(xyz + 3 * q);
+}
+
+// st->first = the first interneuron whose first try is too close to an earlier one's;
+// a warp per interneuron, the longest rows first
+__global__ void __launch_bounds__(kRowThreads) k_i_scan(Geo g, int n_i, const double* xyz, const float4* xyz32,
+                                                        State* st)
+{
+    const int lane = threadIdx.x & 31;
+    const int i = n_i - 1 - (blockIdx.x * (kRowThreads / 32) + (threadIdx.x >> 5));
+    if (i < 1) return;
+    const int first = __shfl_sync(0xffffffffu, *(volatile int*)&st->first, 0);
+    if (i >= first) return;
+    const float4 a = xyz32[i];
+    bool c = false;
+    for (int j = lane; j < i && !c; j += 32) c = close_mixed(g, a, xyz32[j], xyz + 3 * i, xyz + 3 * j);
+    if (__any_sync(0xffffffffu, c) && lane == 0) atomicMin(&st->first, i);
+}
+
+// the sequential part of the interneuron placement (sphere), from the first conflict on:
+// the conflicting interneuron draws again until it fits, then the next conflict among
+// the later ones is searched, until there is none (one block)
+__global__ void __launch_bounds__(1024) k_interneurons(Geo g, int n_i, double* xyz, float4* xyz32, const double* base,
                                                        State* st)
 {
     const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarps = nth >> 5;
-    if (!g.sphere) {
-        // square grid (:231-241): side^2 jittered points; the rest stay at the origin
-        for (int q = tid; q < g.side * g.side; q += nth) {
-            const int i = q / g.side, k = q % g.side;
-            const ug::Philox4 b = ug::stream_block(
-                ug::make_stream(g.seed, ug::kNoiseTopology, g.net, (uint32_t)q, kPartInterneuron), 0);
-            xyz[3 * q] = (double)(i + 1) / (g.root + 1) - kShift * g.model + ug::random_G(2 * kShift * g.model, b.x);
-            xyz[3 * q + 1] =
-                (double)(k + 1) / (g.root + 1) - kShift * g.model + ug::random_G(2 * kShift * g.model, b.y);
-            xyz[3 * q + 2] = 0.0;
-            xyz32[q] = to32(xyz + 3 * q);
-        }
-        for (int q = g.side * g.side + tid; q < n_i; q += nth) xyz32[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-        return;
-    }
-    // the Fibonacci lattice (:296-300), accumulated in the reference's order
-    if (tid == 0) {
-        const double dphi = kPi * (3.0 - sqrt(5.0)), dz = 2 / static_cast<double>(n_i);
-        double phi = 0, z = 1 - dz / 2.0;
-        for (int i = 0; i < n_i; ++i) {
-            base[2 * i] = z;
-            base[2 * i + 1] = phi;
-            z = z - dz;
-            phi = phi + dphi;
-        }
-    }
-    __syncthreads();
-    for (int i = tid; i < n_i; i += nth) {
-        i_try(g, i, 0, base[2 * i], base[2 * i + 1], xyz + 3 * i);
-        xyz32[i] = to32(xyz + 3 * i);
-    }
-    __syncthreads();
     __shared__ int s_first, s_close;
     long long retries = 0;
-    int start = 0;
-    while (start < n_i) {
-        if (tid == 0) s_first = n_i;
-        __syncthreads();
-        // the first pending interneuron whose try is too close to an earlier one
-        for (int i = start + warp; i < n_i; i += nwarps) {
-            const int first = __shfl_sync(0xffffffffu, *(volatile int*)&s_first, 0);
-            if (i >= first) break;
-            const float4 a = xyz32[i];
-            bool c = false;
-            for (int j = lane; j < i && !c; j += 32) c = close_mixed(g, a, xyz32[j], xyz + 3 * i, xyz + 3 * j);
-            if (__any_sync(0xffffffffu, c)) {
-                if (lane == 0) atomicMin(&s_first, i);
-                break;
-            }
-        }
-        __syncthreads();
-        const int f = s_first;
-        if (f >= n_i) break;
+    int f = st->first;
+    while (f < n_i) {
         // every try before it stands; it draws again until it fits
         bool placed = false;
         for (int r = 1; r <= kMaxRetry; ++r) {
@@ -263,7 +258,23 @@ __global__ void __launch_bounds__(1024) k_interneurons(Geo g, int n_i, double* x
             return;
         }
         __syncthreads();
-        start = f + 1;
+        // the first later interneuron whose try is too close to an earlier one
+        if (tid == 0) s_first = n_i;
+        __syncthreads();
+        for (int i = f + 1 + warp; i < n_i; i += nwarps) {
+            const int first = __shfl_sync(0xffffffffu, *(volatile int*)&s_first, 0);
+            if (i >= first) break;
+            const float4 a = xyz32[i];
+            bool c = false;
+            for (int j = lane; j < i && !c; j += 32) c = close_mixed(g, a, xyz32[j], xyz + 3 * i, xyz + 3 * j);
+            if (__any_sync(0xffffffffu, c)) {
+                if (lane == 0) atomicMin(&s_first, i);
+                break;
+            }
+        }
+        __syncthreads();
+        f = s_first;
+        __syncthreads();
     }
     if (tid == 0) st->retries = retries;
 }
@@ -713,8 +724,26 @@ ug_status generate(ug_ctx* ctx, const ug_topology_params& p, int n_ra, int n_i, 
     TCUDA(cudaEventRecord(ev0, st));
     TCUDA(cudaMemsetAsync(dst, 0, sizeof(State), st));
     TCUDA(cudaMemsetAsync(ii, 0, 3 * sizeof(double) * (size_t)n_i, st));
-    k_interneurons<<<1, 1024, 0, st>>>(g, n_i, ii, ii32, base, dst);
+    if (g.sphere) {
+        // the Fibonacci lattice (:296-300), accumulated in the reference's order
+        std::vector<double> lattice(2 * (size_t)n_i);
+        const double dphi = kPi * (3.0 - std::sqrt(5.0)), dz = 2 / static_cast<double>(n_i);
+        double phi = 0, z = 1 - dz / 2.0;
+        for (int i = 0; i < n_i; ++i) {
+            lattice[2 * i] = z;
+            lattice[2 * i + 1] = phi;
+            z = z - dz;
+            phi = phi + dphi;
+        }
+        TCUDA(cudaMemcpyAsync(base, lattice.data(), lattice.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    }
+    k_i_first_tries<<<(n_i + 255) / 256, 256, 0, st>>>(g, n_i, base, ii, ii32, dst);
     ++launches;
+    if (g.sphere) {
+        k_i_scan<<<(n_i + kRowThreads / 32 - 1) / (kRowThreads / 32), kRowThreads, 0, st>>>(g, n_i, ii, ii32, dst);
+        k_interneurons<<<1, 1024, 0, st>>>(g, n_i, ii, ii32, base, dst);
+        launches += 2;
+    }
     TCUDA(cudaGetLastError());
     TCUDA(cudaEventRecord(ev_i, st));
 
@@ -833,9 +862,11 @@ ug_status generate(ug_ctx* ctx, const ug_topology_params& p, int n_ra, int n_i, 
     if (n_tr > 0) {
         std::vector<double> d(n_ra - 1);
         for (int i = 1; i < n_ra; ++i) d[i - 1] = host_dist(g, &t.ra_xyz[0], &t.ra_xyz[3 * (size_t)i]);
+        // the n_tr - 1 nearest, in order of distance (ties by index)
         std::vector<int> idx(d.size());
         std::iota(idx.begin(), idx.end(), 0);
-        std::stable_sort(idx.begin(), idx.end(), [&d](int a, int b) { return d[a] < d[b]; });
+        std::partial_sort(idx.begin(), idx.begin() + (n_tr - 1), idx.end(),
+                          [&d](int a, int b) { return d[a] < d[b] || (d[a] == d[b] && a < b); });
         for (int i = 1; i < n_tr; ++i) t.clustered[i] = idx[i - 1] + 1;
         std::vector<int> unsampled(n_ra);
         std::iota(unsampled.begin(), unsampled.end(), 0);
