@@ -311,6 +311,23 @@ ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint32_t trial,
                                     int32_t* soma_first, int32_t* dend_count, int32_t* dend_first,
                                     int32_t* inter_count, int32_t* inter_first);
 
+/* ---- Inhibition tracking (the growth variant with_inhibition_tracking) -----------------
+ * trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking
+ * (NetworkGrowthSimulator.cpp:8085-8838) is the growth trial plus a record of every HVC(RA)
+ * neuron's inhibitory dendritic conductance Ginh_d: at the trial's start and at the first
+ * step at or after each multiple of the resolution (:8158-8160, :8432-8442), in
+ * int(TRIAL_DURATION / resolution) points.  While set, every growth trial of the network
+ * (alone or in a group) records; test trials do not.  resolution_ms 0 switches it off. */
+ug_status ug_set_inhibition_tracking(ug_ctx* ctx, int32_t net_id, double resolution_ms);
+/* The record of the last growth trial, [n_ra][num_points] (the layout of Ginh_global and of
+ * Ginh_trial_<trial>.bin), and the resolution; out may be NULL to query the sizes. */
+ug_status ug_get_inhibitory_conductance(ug_ctx* ctx, int32_t net_id, double* out, int32_t* num_points,
+                                        double* resolution_ms);
+/* write_inhibition_tracking_state (:18606-18618): num_synapses_<trial>.bin,
+ * spike_times_{soma,dend,interneuron}_<trial>.bin and Ginh_trial_<trial>.bin
+ * (write_inhibitory_conductance :17689-17709) into dir. */
+ug_status ug_write_inhibition_tracking_state(ug_ctx* ctx, int32_t net_id, const char* dir, int32_t trial_number);
+
 /* ---- Network topology generation (createNetworkForGrowth) ----------------------------
  * generate_network_topology (NetworkGrowthSimulator.cpp:110-155) on the device:
  * sample_coordinates (:222-403), sample_connections (:620-705) with p_RA2I / p_I2RA

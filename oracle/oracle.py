@@ -290,6 +290,20 @@ class OracleNet:
             out.append(buf.reshape(-1, k, width) if k else buf)
         return out
 
+    def set_inhibition_tracking(self, resolution: float):
+        self.L.ugo_set_inhibition_tracking.argtypes = [C.c_void_p, C.c_double]
+        self.L.ugo_set_inhibition_tracking(self.h, resolution)
+
+    def inhibition(self):
+        """The last trial's Ginh_d record, [n_ra][points]."""
+        L = self.L
+        L.ugo_get_inhibition.restype = C.c_int32
+        L.ugo_get_inhibition.argtypes = [C.c_void_p, _f64p, C.c_int64]
+        points = L.ugo_get_inhibition(self.h, None, 0)
+        out = np.zeros((self.n_ra, points))
+        L.ugo_get_inhibition(self.h, _ptr(out, _f64p), out.size)
+        return out
+
     def set_delivery_log(self, on=True):
         self.L.ugo_set_delivery_log(self.h, 1 if on else 0)
 

@@ -481,6 +481,8 @@ struct ugo_net {
 
     std::vector<int> trace_ra, trace_i;
     std::vector<double> trace_ra_buf, trace_i_buf;
+    double ginh_res;                              /* inhibition tracking resolution (0: off) */
+    std::vector<double> ginh;                     /* [n_ra][points] Ginh_d record (Ginh_global) */
     bool log_deliveries;
     std::vector<int> delivery_log;
 
@@ -646,6 +648,14 @@ int run_trial(ugo_net* net, bool growth, bool training, uint32_t trial)
     const int num_steps = net->num_steps;
 
     if (!net->trace_ra.empty() || !net->trace_i.empty()) record_traces(net);
+    /* inhibition tracking (:8158-8160): Ginh_d at the trial's start, then at the first step
+     * at or after each multiple of the resolution (:8432-8442) */
+    const int ginh_points = net->ginh_res > 0 ? (int)(num_steps * TIMESTEP / net->ginh_res) : 0;
+    int ginh_pos = 1;
+    if (ginh_points > 0) {
+        if (net->ginh.size() != (size_t)NRA * ginh_points) net->ginh.assign((size_t)NRA * ginh_points, 0.0);
+        for (int i = 0; i < NRA; ++i) net->ginh[(size_t)i * ginh_points] = net->ra[i].Ginh_d;
+    }
 
     for (int t = 1; t < num_steps; ++t) {
         internal_time += TIMESTEP;
@@ -772,6 +782,11 @@ int run_trial(ugo_net* net, bool growth, bool training, uint32_t trial)
                 net->spk_dend_n.push_back(i);
                 net->spk_dend_s.push_back(t);
             }
+        }
+        if (ginh_points > 0 && internal_time >= static_cast<double>(ginh_pos) * net->ginh_res) {
+            if (ginh_pos < ginh_points)
+                for (int i = 0; i < NRA; ++i) net->ginh[(size_t)i * ginh_points + ginh_pos] = net->ra[i].Ginh_d;
+            ginh_pos += 1;
         }
 
         for (int i = 0; i < NI; ++i) {
@@ -1084,6 +1099,7 @@ ugo_net* ugo_new(int32_t n_ra, int32_t n_i)
     net->n_ra = n_ra;
     net->n_i = n_i;
     net->num_steps = (int)(TRIAL_DURATION / TIMESTEP);
+    net->ginh_res = 0.0;
     net->seed = 0;
     net->net_id = 0;
     std::memset(&net->syn, 0, sizeof(net->syn));
@@ -1193,6 +1209,20 @@ void ugo_set_activity_history(ugo_net* net, const int32_t* hist)
 {
     const int W = net->mat.RATE_WINDOW_LONG;
     for (int i = 0; i < net->n_ra; ++i) net->hist[i].assign(hist + (size_t)i * W, hist + (size_t)(i + 1) * W);
+}
+
+void ugo_set_inhibition_tracking(ugo_net* net, double resolution)
+{
+    net->ginh_res = resolution > 0 ? resolution : 0.0;
+    net->ginh.clear();
+}
+
+int32_t ugo_get_inhibition(const ugo_net* net, double* out, int64_t capacity)
+{
+    if (net->ginh_res <= 0 || net->n_ra == 0) return 0;
+    const int32_t points = (int32_t)(net->ginh.size() / (size_t)net->n_ra);
+    if (out && capacity >= (int64_t)net->ginh.size()) std::memcpy(out, net->ginh.data(), net->ginh.size() * sizeof(double));
+    return points;
 }
 
 void ugo_set_trace(ugo_net* net, int32_t nra, const int32_t* ra_ids, int32_t ni, const int32_t* i_ids)

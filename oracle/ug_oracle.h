@@ -89,6 +89,14 @@ void ugo_set_trace(ugo_net* net, int32_t n_ra_traced, const int32_t* ra_ids, int
                    const int32_t* i_ids);
 int64_t ugo_get_trace(const ugo_net* net, int32_t which, double* out, int64_t capacity);
 
+/* Inhibition tracking (trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking,
+ * NetworkGrowthSimulator.cpp:8085-8838): every trial records each HVC(RA) neuron's Ginh_d at its
+ * start and at the first step at or after each multiple of `resolution` ms (0: off).  The record
+ * is [n_ra][points], points = (int)(trial duration / resolution); ugo_get_inhibition returns points
+ * and copies the record when capacity allows. */
+void ugo_set_inhibition_tracking(ugo_net* net, double resolution);
+int32_t ugo_get_inhibition(const ugo_net* net, double* out, int64_t capacity);
+
 /* Record every RA->RA delivery (source, target, step) of the next trial (debug parity). */
 void ugo_set_delivery_log(ugo_net* net, int32_t enabled);
 int64_t ugo_get_delivery_log(const ugo_net* net, int32_t* out3, int64_t capacity);

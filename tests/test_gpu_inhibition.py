@@ -1,0 +1,148 @@
+"""Inhibition tracking on the device (ug_set_inhibition_tracking: the growth variant
+trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking,
+c++/src/NetworkGrowthSimulator.cpp:8085-8838) against the oracle.
+
+Double build: the Ginh_d record of every growth trial equal to the oracle's within
+1e-10 mS/cm^2, alone and as a member of a group (the device sums the kicks of a
+synchronisation in 64-bit fixed point, 2^-40 units, so each inhibitory event may
+differ from the oracle's double sum by up to 5e-13).  Single build: the same record within 1e-2 relative (1e-4
+mS/cm^2 absolute) for at least 95 % of the samples; a spike one step apart shifts
+an inhibitory kick by a step.  write_inhibition_tracking_state's files and
+`ug_growth chainGrowth --track-inhibition` give the same records."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleNet
+from tests.test_gpu_cli import topology  # noqa: F401  (the program test's network directory)
+from tests.test_gpu_growth import growth_net
+from unsupervised_growth_gb300 import files as F
+
+pytestmark = pytest.mark.gpu
+
+TRIALS = 2
+FIX_TOL = 1e-10   # fixed-point kick sums: up to 5e-13 per event
+
+
+@pytest.fixture(scope="module")
+def oracle_records():
+    out = {}
+    for res in (0.5, 0.37):
+        o = OracleNet(growth_net())
+        o.set_inhibition_tracking(res)
+        recs = []
+        for t in range(TRIALS):
+            assert o.run_trial(True, t) == 0
+            recs.append(o.inhibition())
+            o.after_growth_trial(t)
+        out[res] = recs
+    assert out[0.5][0].max() > 0
+    return out
+
+
+@pytest.mark.parametrize("res", [0.5, 0.37])
+def test_fp64_matches_oracle(engine64, oracle_records, res):
+    rn = engine64.load_network(growth_net())
+    rn.set_inhibition_tracking(res)
+    for t in range(TRIALS):
+        rn.run_growth_trials(t, 1, True)
+        rec, r = rn.inhibitory_conductance()
+        assert r == res and rec.shape == oracle_records[res][t].shape
+        np.testing.assert_allclose(rec, oracle_records[res][t], rtol=0, atol=FIX_TOL)
+    rn.free()
+
+
+def test_fp32_close(engine32, oracle_records):
+    rn = engine32.load_network(growth_net())
+    rn.set_inhibition_tracking(0.5)
+    for t in range(TRIALS):
+        rn.run_growth_trials(t, 1, True)
+        rec, _ = rn.inhibitory_conductance()
+        close = np.isclose(rec, oracle_records[0.5][t], rtol=1e-2, atol=1e-4)
+        assert close.mean() > 0.95, close.mean()
+    rn.free()
+
+
+def test_switch_off_and_test_trials(engine64):
+    from unsupervised_growth_gb300.engine import UGError
+    rn = engine64.load_network(growth_net())
+    with pytest.raises(UGError):
+        rn.inhibitory_conductance()                  # never set
+    rn.set_inhibition_tracking(0.5)
+    with pytest.raises(UGError):
+        rn.inhibitory_conductance()                  # no growth trial yet
+    rn.run_test_trials(0, 2)                         # test trials do not record
+    with pytest.raises(UGError):
+        rn.inhibitory_conductance()
+    rn.run_growth_trials(0, 1, True)
+    a, _ = rn.inhibitory_conductance()
+    rn.set_inhibition_tracking(0)
+    rn.run_growth_trials(1, 1, True)
+    with pytest.raises(UGError):
+        rn.inhibitory_conductance()
+    with pytest.raises(UGError):
+        rn.set_inhibition_tracking(-1.0)
+    assert a.max() > 0
+    rn.free()
+
+
+def test_group_member(engine64, oracle_records):
+    """A tracked network grown in a group beside an untracked one records what it records alone."""
+    a = engine64.load_network(growth_net())
+    b = engine64.load_network(growth_net(seed=9))
+    a.set_inhibition_tracking(0.5)
+    for t in range(TRIALS):
+        engine64.run_group([(a, "growth", t, 1, True), (b, "growth", t, 1, True)])
+        rec, _ = a.inhibitory_conductance()
+        np.testing.assert_allclose(rec, oracle_records[0.5][t], rtol=0, atol=FIX_TOL)
+    a.free()
+    b.free()
+
+
+def test_files(engine64, tmp_path):
+    """write_inhibition_tracking_state's files."""
+    rn = engine64.load_network(growth_net())
+    rn.set_inhibition_tracking(0.5)
+    rn.run_growth_trials(0, 1, True)
+    rn.write_inhibition_tracking_state(str(tmp_path), 0)
+    g, res = F.read_inhibitory_conductance(str(tmp_path / "Ginh_trial_0.bin"))
+    rec, _ = rn.inhibitory_conductance()
+    assert res == 0.5 and np.array_equal(g, rec)
+    rec3 = np.fromfile(tmp_path / "num_synapses_0.bin", dtype="<i4")
+    assert rec3.tolist()[0] == 0 and len(rec3) == 3
+    times, trial, _ = F.read_spike_times(str(tmp_path / "spike_times_soma_0.bin"))
+    n, s = rn.spikes(0, 0)
+    assert trial == 0 and sum(len(x) for x in times) == len(n)
+    for name in ("spike_times_dend_0.bin", "spike_times_interneuron_0.bin"):
+        assert (tmp_path / name).exists()
+    rn.free()
+
+
+def test_program_track_inhibition(topology, tmp_path):
+    """ug_growth chainGrowth --track-inhibition: the variant's files every trial, the full
+    state every --save-long trials; trial 2 continued from the trial-1 state through the
+    C ABI gives the same record."""
+    import subprocess
+
+    from unsupervised_growth_gb300 import build as B
+    from unsupervised_growth_gb300.engine import Engine
+    root, topo, train, cfg = topology
+    out = tmp_path / "track"
+    out.mkdir()
+    r = subprocess.run([B.CLI, "chainGrowth", f"{topo}/", str(train), str(cfg), f"{out}/", "--trials", "3",
+                        "--save-long", "1", "--precision", "64", "--track-inhibition", "1.0"],
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    for t in (0, 1):
+        for name in (f"Ginh_trial_{t}.bin", f"num_synapses_{t}.bin", f"spike_times_soma_{t}.bin",
+                     f"spike_times_dend_{t}.bin", f"spike_times_interneuron_{t}.bin", f"weights_{t}.bin"):
+            assert (out / name).exists(), name
+    assert not (out / "RA_RA_active_connections.bin").exists()   # no graph-state saves in this variant
+    eng = Engine(precision=64, spike_capacity_per_neuron=256)
+    rn = eng.load_network_dir(f"{out}/", 1, seed=15000)
+    rn.set_inhibition_tracking(1.0)
+    rn.run_growth_trials(2, 1, True)
+    g, res = F.read_inhibitory_conductance(str(out / "Ginh_trial_2.bin"))
+    rec, _ = rn.inhibitory_conductance()
+    assert res == 1.0 and g.shape == (rn.net.n_ra, 500)
+    np.testing.assert_array_equal(g, rec)
+    rn.free()

@@ -13,7 +13,10 @@
 // --precision 32|64, --device D, --seed S (noise streams; 15000 by default),
 // --spike-capacity C (spikes recorded per neuron and trial for the spike files);
 // createNetworkForGrowth takes --n-ra, --n-i, --n-tr (2000, 550 and 10, the sizes its
-// reference main hard-codes), --seed and --device.
+// reference main hard-codes), --seed and --device.  --track-inhibition R (ms) makes the
+// growth programs run the inhibition-tracking variant (new_chain_growth_with_inhibition_tracking,
+// NetworkGrowthSimulator.cpp:1784-1862): every trial records each HVC(RA) neuron's Ginh_d every
+// R ms and writes write_inhibition_tracking_state's files; the full state every --save-long trials.
 //
 // Growth saves are written after a trial's between-trial bookkeeping, so
 // continueChainGrowth from a saved trial T runs trials T + 1, T + 2, ...
@@ -31,6 +34,7 @@ struct Opts {
     long trials = -1;
     int save_short = -1, save_long = -1, precision = 32, device = 0, spikes = 256;
     int n_ra = 2000, n_i = 550, n_tr = 10;
+    double track = 0.0;   // inhibition tracking resolution (ms), 0: off
     unsigned long long seed = 15000;
 };
 
@@ -53,6 +57,7 @@ bool parse_opts(int argc, char** argv, int first, Opts& o)
         else if (a == "--n-ra") o.n_ra = std::atoi(v);
         else if (a == "--n-i") o.n_i = std::atoi(v);
         else if (a == "--n-tr") o.n_tr = std::atoi(v);
+        else if (a == "--track-inhibition") o.track = std::atof(v);
         else {
             std::fprintf(stderr, "unknown option %s\n", a.c_str());
             return false;
@@ -75,9 +80,12 @@ std::string path(const std::string& dir, const std::string& name)
 
 // chain_growth (NetworkGrowthSimulator.cpp:5731-5845): a growth trial, then the graph
 // state every save_short trials and the full state every save_long trials.
+// chain_growth_with_inhibition_tracking (:5662-5729): the full state every save_long
+// trials and the inhibition-tracking state after every trial.
 int grow(ug_ctx* ctx, int net, long first, const Opts& o, const std::string& out)
 {
     const long last = o.trials < 0 ? (1L << 30) : first + o.trials;
+    if (o.track > 0 && check(ug_set_inhibition_tracking(ctx, net, o.track), "inhibition tracking")) return 1;
     for (long t = first; t < last; ++t) {
         const ug_status s = ug_run_growth_trials(ctx, net, (uint32_t)t, 1, 1);
         if (s == UG_ENUMERIC) {
@@ -86,6 +94,15 @@ int grow(ug_ctx* ctx, int net, long first, const Opts& o, const std::string& out
         }
         if (check(s, "growth trial")) return 1;
         std::printf("Trial %ld\n", t);
+        if (o.track > 0) {
+            if (t % o.save_long == 0 &&
+                check(ug_write_state_dir(ctx, net, out.c_str(), ("_" + std::to_string(t)).c_str(), (int32_t)t),
+                      "full state"))
+                return 1;
+            if (check(ug_write_inhibition_tracking_state(ctx, net, out.c_str(), (int32_t)t), "inhibition tracking state"))
+                return 1;
+            continue;
+        }
         if (t % o.save_short == 0 && check(ug_write_graph_state(ctx, net, out.c_str(), (int32_t)t), "graph state"))
             return 1;
         if (t % o.save_long == 0 &&
@@ -105,6 +122,7 @@ int usage()
                  "  ug_growth continueChainGrowth <data dir> <output dir> <starting trial> [options]\n"
                  "  ug_growth chainTest <network dir> <trial number> <number of test trials> <output dir> [options]\n"
                  "options: --trials N --save-short K --save-long K --precision 32|64 --device D --seed S\n"
+                 "         --track-inhibition R (the inhibition-tracking growth variant, Ginh_d every R ms)\n"
                  "         --spike-capacity C (spikes recorded per neuron and trial, 256 by default)\n");
     return 2;
 }

@@ -754,6 +754,34 @@ ug_status ug_write_graph_state(ug_ctx* ctx, int32_t net, const char* dir_c, int3
     return UG_OK;
 }
 
+// write_inhibition_tracking_state (:18606-18618)
+ug_status ug_write_inhibition_tracking_state(ug_ctx* ctx, int32_t net, const char* dir_c, int32_t trial_number)
+{
+    if (!ctx || !dir_c) return ferr(UG_EINVAL, "null argument");
+    const std::string dir(dir_c), e = "_" + std::to_string(trial_number);
+    ug_network_info info;
+    UG_FTRY(ug_get_network_info(ctx, net, &info));
+    const int n = info.n_ra;
+    int32_t points = 0;
+    double res = 0.0;
+    UG_FTRY(ug_get_inhibitory_conductance(ctx, net, nullptr, &points, &res));
+    std::vector<double> g((size_t)n * points);
+    UG_FTRY(ug_get_inhibitory_conductance(ctx, net, g.data(), &points, &res));
+    // write_num_synapses: a new file at trial 0, appended to afterwards (:17885-17912)
+    UG_FTRY(ug_append_num_synapses(ctx, net, join(dir, "num_synapses" + e + ".bin").c_str(), trial_number));
+    UG_FTRY(write_spikes(ctx, net, 0, n, trial_number, join(dir, "spike_times_soma" + e + ".bin")));
+    UG_FTRY(write_spikes(ctx, net, 1, n, trial_number, join(dir, "spike_times_dend" + e + ".bin")));
+    UG_FTRY(write_spikes(ctx, net, 2, info.n_i, trial_number, join(dir, "spike_times_interneuron" + e + ".bin")));
+    // write_inhibitory_conductance (:17689-17709)
+    const std::string p = join(dir, "Ginh_trial" + e + ".bin");
+    Out o(p, false);
+    o.put((int32_t)n);
+    o.put(points);
+    o.put(res);
+    o.put(g.data(), g.size());
+    return closed(o, p);
+}
+
 }  // extern "C"
 
 namespace {

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kBlock) kl_noise_events(const GroupMember<R>* 
 // act_cnt: the group's row-queue counters (null without growth members); the
 // counter of the next interval's queue is cleared here, after the row kernel
 // of the previous interval has read it.
-template <class R>
+template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? UG_RA_MIN_BLOCKS : 1)
     kl_interval_ra(const GroupMember<R>* members, const int4* items, const int* count, int* act_cnt, int q, int s0,
                    int s1)
@@ -93,8 +93,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? UG_RA_MIN_BLOCKS : 1)
         act_cnt[2 + ((q + 1) & 1)] = 0; // row kernels of the previous one
     }
     for_items(members, items, *count, M, [&](const GroupMember<R>& m, int bx, int by) {
-        if constexpr (sizeof(R) == 4) interval_ra_x2_body(m.n, m.bt, q, s0, s1, m.rc, bx, by);
-        else interval_ra_body(m.n, m.bt, q, s0, s1, m.rc, bx, by);
+        if constexpr (sizeof(R) == 4) interval_ra_x2_body<R, kTrack>(m.n, m.bt, q, s0, s1, m.rc, bx, by);
+        else interval_ra_body<R, kTrack>(m.n, m.bt, q, s0, s1, m.rc, bx, by);
     });
 }
 

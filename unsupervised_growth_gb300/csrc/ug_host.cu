@@ -171,6 +171,10 @@ public:
     // since they were last uploaded.
     virtual bool f32_view(ug::NetDev<float>* out) const { (void)out; return false; }
     virtual int batch() const = 0;   // instances of the last batch
+    // Inhibition tracking of growth trials (resolution 0: off) and the last record,
+    // [n_ra][points] (points only when out is null).
+    virtual ug_status set_inhibition_tracking(double resolution, cudaStream_t st) = 0;
+    virtual ug_status inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st) = 0;
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -242,6 +246,8 @@ public:
     size_t device_bytes() const;
     size_t footprint(int kind, int B) const;
     int batch() const override { return B_; }
+    ug_status set_inhibition_tracking(double resolution, cudaStream_t st) override;
+    ug_status inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st) override;
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -288,6 +294,13 @@ private:
         gNewpostCnt_, gSomaBits_, gBad_, gRep_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
+    // inhibition tracking
+    double ginh_res_ = 0.0;
+    int ginh_points_ = 0;
+    int ginh_gen_ = 0;             // changes whenever tracking is switched or resized
+    int ggraph_ginh_gen_ = -1;     // the generation the growth graph was captured with
+    bool ginh_recorded_ = false;   // a growth trial has recorded since tracking was set
+    DevMem gGinh_, gGinhSlot_;
     std::vector<int> syncidx_;
     std::vector<double> ra_decay_, i_decay_;
     double max_delay_ = 0.0;   // bound on every delay, including those a replaced neuron can get
@@ -663,6 +676,8 @@ ug_status NetImpl<R>::prepare_test(uint32_t first_trial, int n_trials, cudaStrea
     if (rara_dirty_) UG_TRY(sync_static_lists(st));
     UG_TRY(ensure_batch(n_trials));
     bd_.soma_bits = nullptr;
+    bd_.ginh_rec = nullptr;
+    bd_.ginh_slot = nullptr;
     bd_.B = n_trials;
     bd_.kick_on = 1;
     bd_.scatter_rara = 1;
@@ -875,7 +890,7 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
         if (!graphs || lc.timer) {
             UG_TRY(issue_growth_trial(lc, launches));
         } else {
-            if (!ggraph_ || ggraph_training_ != bd_.kick_on) {
+            if (!ggraph_ || ggraph_training_ != bd_.kick_on || ggraph_ginh_gen_ != ginh_gen_) {
                 if (ggraph_) cudaGraphExecDestroy(ggraph_);
                 ggraph_ = nullptr;
                 cudaStream_t cap;
@@ -894,6 +909,7 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
                 cudaGraphDestroy(g);
                 UG_CUDA(e);
                 ggraph_training_ = bd_.kick_on;
+                ggraph_ginh_gen_ = ginh_gen_;
             }
             UG_CUDA(cudaGraphLaunch(ggraph_, st));
             int64_t n = 0;
@@ -921,6 +937,9 @@ ug_status NetImpl<R>::prepare_growth(uint32_t trial, int training, cudaStream_t 
     bd_.kick_on = training ? 1 : 0;
     bd_.scatter_rara = 0;
     bd_.soma_bits = gSomaBits_.as<int>();
+    bd_.ginh_rec = ginh_res_ > 0 ? gGinh_.as<R>() : nullptr;
+    bd_.ginh_slot = ginh_res_ > 0 ? gGinhSlot_.as<int>() : nullptr;
+    if (ginh_res_ > 0) ginh_recorded_ = true;
     B_ = 1;
     UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
     // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
@@ -929,6 +948,57 @@ ug_status NetImpl<R>::prepare_growth(uint32_t trial, int training, cudaStream_t 
     UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), &trial, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), &mean_inj, sizeof(double), cudaMemcpyHostToDevice, st));
     UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+// trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking (:8085-8838):
+// Ginh_d of every HVC(RA) neuron at the trial's start (:8158-8160) and at the first step at
+// or after each multiple of the resolution (:8432-8442), into int(TRIAL_DURATION /
+// resolution) points (initialize_global_inhibitory_conductances :16160-16170).  Points not
+// reached in a trial keep their earlier values, as the reference's arrays do.
+template <class R>
+ug_status NetImpl<R>::set_inhibition_tracking(double resolution, cudaStream_t st)
+{
+    if (!(resolution >= 0.0)) return fail(UG_EINVAL, "the resolution must be >= 0");
+    ++ginh_gen_;
+    ginh_recorded_ = false;
+    if (resolution == 0.0) {
+        ginh_res_ = 0.0;
+        ginh_points_ = 0;
+        return UG_OK;
+    }
+    const int points = (int)(h.num_steps * kTimestep / resolution);
+    if (points < 1) return fail(UG_EINVAL, "the resolution is longer than the trial");
+    std::vector<int> slot(h.num_steps, -1);
+    int pos = 1;
+    for (int st_ = 1; st_ < h.num_steps; ++st_)
+        if (T[st_] >= static_cast<double>(pos) * resolution) {
+            if (pos < points) slot[st_] = pos;
+            ++pos;
+        }
+    UG_TRY(gGinhSlot_.upload(slot, st));
+    UG_TRY(gGinh_.alloc((size_t)points * h.n_ra * sizeof(R)));
+    UG_CUDA(cudaMemsetAsync(gGinh_.as<R>(), 0, (size_t)points * h.n_ra * sizeof(R), st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    ginh_res_ = resolution;
+    ginh_points_ = points;
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st)
+{
+    if (ginh_res_ <= 0) return fail(UG_EINVAL, "inhibition tracking is off for this network");
+    if (!ginh_recorded_) return fail(UG_EINVAL, "no growth trial has run since inhibition tracking was set");
+    if (points) *points = ginh_points_;
+    if (resolution) *resolution = ginh_res_;
+    if (!out) return UG_OK;
+    const int n = h.n_ra, P = ginh_points_;
+    std::vector<R> rec((size_t)P * n);
+    UG_CUDA(cudaMemcpyAsync(rec.data(), gGinh_.as<R>(), rec.size() * sizeof(R), cudaMemcpyDeviceToHost, st));
+    UG_CUDA(cudaStreamSynchronize(st));
+    for (int i = 0; i < n; ++i)
+        for (int p = 0; p < P; ++p) out[(size_t)i * P + p] = (double)rec[(size_t)p * n + i];
     return UG_OK;
 }
 
@@ -1278,7 +1348,7 @@ private:
     int num_steps_ = -1;
     int ra_bps_ = -1, i_bps_ = -1;
     ug::GroupDev dev_{};
-    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // [with growth members]
+    cudaGraphExec_t graph_[4] = {};   // [with growth members + 2 with inhibition tracking]
 };
 
 template <class R>
@@ -1387,14 +1457,17 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
     dev_.act_cap = act_cap;
     dev_.bad = bad_.as<int>();
     dev_.T = T_.as<double>();
-    // launch: one captured graph per kind (with or without growth members),
-    // reused across compositions
+    dev_.track = 0;
+    for (const ug::GroupMember<R>& m : hmem_)
+        if (m.bt.ginh_slot) dev_.track = 1;
+    // launch: one captured graph per kind (with or without growth members, with or
+    // without inhibition tracking), reused across compositions
     const int64_t Q = (int64_t)sync_steps.size();
     const int64_t n_launch = 2 + (sizeof(R) == 4 ? 1 : 0) + 2 * (Q + 1) + (growth ? 4 * Q + 2 : 0);
     if (!graphs || lc.timer) {
         UG_CUDA(ug::launch_group_trial<R>(dev_, sync_steps, num_steps, growth, lc, nullptr));
     } else {
-        cudaGraphExec_t& ge = graph_[growth ? 1 : 0];
+        cudaGraphExec_t& ge = graph_[(growth ? 1 : 0) + (dev_.track ? 2 : 0)];
         if (!ge) {
             cudaStream_t cap;
             UG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
@@ -2199,6 +2272,25 @@ ug_status ug_launch_count(ug_ctx* ctx, int64_t* out)
     if (!ctx || !out) return fail(UG_EINVAL, "null argument");
     *out = ctx->launches;
     return UG_OK;
+}
+
+ug_status ug_set_inhibition_tracking(ug_ctx* ctx, int32_t net_id, double resolution_ms)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    return n->set_inhibition_tracking(resolution_ms, ctx->stream);
+}
+
+ug_status ug_get_inhibitory_conductance(ug_ctx* ctx, int32_t net_id, double* out, int32_t* num_points,
+                                        double* resolution_ms)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    return n->inhibition(out, num_points, resolution_ms, ctx->stream);
 }
 
 }  // extern "C"

@@ -59,7 +59,10 @@ inline void launch_ra(const NetDev<double>& n, const BatchDev<double>& b, int q,
 {
     const dim3 g((n.n_ra + kBlock - 1) / kBlock, b.B);
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
-    k_interval_ra<double><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    if (b.ginh_slot)
+        k_interval_ra<double, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    else
+        k_interval_ra<double><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
     if (lc.timer) lc.timer->end(lc.main);
 }
 
@@ -68,7 +71,10 @@ inline void launch_ra(const NetDev<float>& n, const BatchDev<float>& b, int q, i
 {
     const dim3 g(((n.n_ra + 1) / 2 + kBlock - 1) / kBlock, b.B);
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
-    k_interval_ra_x2<float><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    if (b.ginh_slot)
+        k_interval_ra_x2<float, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+    else
+        k_interval_ra_x2<float><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
     if (lc.timer) lc.timer->end(lc.main);
 }
 
@@ -234,7 +240,10 @@ cudaError_t launch_group_trial(const GroupDev& d, const std::vector<int>& sync_s
             if (e == cudaSuccess) e = cudaStreamWaitEvent(lc.side, lc.fork, 0);
             if (e != cudaSuccess) return e;
         }
-        UG_TIMED(lc, "k_interval_ra", (kl_interval_ra<R><<<d.grid[kListRA], kBlock, 0, lc.main>>>(mem, d.items[kListRA], c + kListRA, growth ? d.act_cnt : nullptr, q, s0, s1)));
+        if (d.track)
+            UG_TIMED(lc, "k_interval_ra", (kl_interval_ra<R, true><<<d.grid[kListRA], kBlock, 0, lc.main>>>(mem, d.items[kListRA], c + kListRA, growth ? d.act_cnt : nullptr, q, s0, s1)));
+        else
+            UG_TIMED(lc, "k_interval_ra", (kl_interval_ra<R><<<d.grid[kListRA], kBlock, 0, lc.main>>>(mem, d.items[kListRA], c + kListRA, growth ? d.act_cnt : nullptr, q, s0, s1)));
         if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
         kl_interval_i<R><<<d.grid[kListI], kBlock, 0, fork ? lc.side : lc.main>>>(mem, d.items[kListI], c + kListI, q, s0, s1);
         if (lc.timer) lc.timer->end(lc.main);

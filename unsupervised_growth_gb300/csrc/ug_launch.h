@@ -141,6 +141,7 @@ struct GroupDev {
     const double* T = nullptr;                // the group's time grid
     int grid[kNumLists + 2] = {};             // blocks of each list kernel; [kNumLists] row kernel, [+1] heavy rows
     int fork = 1;                             // interneuron kernel on the side stream, beside the RA kernel
+    int track = 0;                            // a member records Ginh_d (inhibition tracking)
 };
 
 // Occupancy-sized grids of the list kernels (call outside stream capture);

@@ -94,6 +94,10 @@ struct BatchDev {
     int member;                // index of this batch in its group
     const int* live_streams;   // [B][n_ra] open delivery streams of each row (the growth state)
     int heavy;                 // block path: 0 never, 1 rows that spiked, 2 every queued row
+    // Inhibition tracking (growth trials): Ginh_d of every HVC(RA) neuron at the trial's start
+    // (slot 0) and after each step st with ginh_slot[st] > 0, in that slot.
+    R* ginh_rec;               // [points][B][n_ra], or null
+    const int* ginh_slot;      // [num_steps] slot recorded after step st, or -1
 };
 
 // Queues row x of a group growth member for interval q if it has deliveries to make.
@@ -274,6 +278,7 @@ __device__ __forceinline__ void trial_init_body(const NetDev<R>& n, const BatchD
                             R(0.00055429), R(0.00000261762353), R(0.01689572), R(0), R(0)};
 #pragma unroll
         for (int k = 0; k < 10; ++k) bt.ra[k][x] = rest[k];
+        if (bt.ginh_rec) bt.ginh_rec[x] = rest[9];   // inhibition tracking, slot 0: Ginh_d at the trial's start
         bt.ra_flags[x] = 0;
         // training kick: first step with internal_time > spread + mean injection time
         // (NetworkGrowthSimulator.cpp:8933-8940, test trial :12815-12823)
@@ -326,7 +331,9 @@ __global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> 
 // by sync q) for every RA neuron of every instance, then scatters the RA->I
 // kicks (and, in test trials, the RA->RA kicks over the static active lists)
 // of the interval's somatic spikes.
-template <class R>
+// kTrack: record Ginh_d for inhibition tracking (a kernel of its own, so that the
+// integrators without tracking carry none of it).
+template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                  const RAStep<R>& rc, int bx, int b)
 {
@@ -361,6 +368,12 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
             ra_step(s, flags, fs, fd, EL, GdCa, p, sid, (uint32_t)st);
             soma |= (uint32_t)fs << (st - s0);
             dend |= (uint32_t)fd << (st - s0);
+            if constexpr (kTrack) {   // inhibition tracking; a group may mix tracked and untracked members
+                if (bt.ginh_slot) {
+                    const int sl = bt.ginh_slot[st];
+                    if (sl > 0) bt.ginh_rec[(size_t)sl * bt.B * n.n_ra + x] = s.Gi;
+                }
+            }
         }
         bt.ra[0][x] = s.Vs; bt.ra[1][x] = s.Vd; bt.ra[2][x] = s.n; bt.ra[3][x] = s.h; bt.ra[4][x] = s.l;
         bt.ra[5][x] = s.r; bt.ra[6][x] = s.c; bt.ra[7][x] = s.Ca; bt.ra[8][x] = s.Ge; bt.ra[9][x] = s.Gi;
@@ -387,17 +400,17 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
                      bt.ring_ra_exc, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
 }
 
-template <class R>
+template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
                                                                                RAStep<R> rc)
 {
-    interval_ra_body(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
+    interval_ra_body<R, kTrack>(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // Single-precision HVC(RA) part of one interval, two neurons per thread
 // (neurons 2t and 2t+1) so that every floating-point instruction of the
 // integrator is a packed f32x2 operation.
-template <class R>
+template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                     const RAStep<R>& rc, int bx, int b)
 {
@@ -464,6 +477,16 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
             ra_debrabant_x2(s, Ge, Gi, P, rc, make_float2(ra_point_f(w0.x), ra_point_f(w1.x)),
                             make_float2(ra_point_f(w0.y), ra_point_f(w1.y)), make_float2(ra_point_f(w0.z), ra_point_f(w1.z)),
                             make_float2(ra_point_f(w0.w), ra_point_f(w1.w)));
+            if constexpr (kTrack) {   // inhibition tracking; a group may mix tracked and untracked members
+                if (bt.ginh_slot) {
+                    const int sl = bt.ginh_slot[st];
+                    if (sl > 0) {
+                        R* rec = bt.ginh_rec + (size_t)sl * bt.B * n.n_ra;
+                        rec[x0] = Gi.x;
+                        if (v1) rec[x1] = Gi.y;
+                    }
+                }
+            }
         }
         bt.ra[0][x0] = s.Vs.x; bt.ra[1][x0] = s.Vd.x; bt.ra[2][x0] = s.n.x; bt.ra[3][x0] = s.h.x; bt.ra[4][x0] = s.l.x;
         bt.ra[5][x0] = s.r.x; bt.ra[6][x0] = s.c.x; bt.ra[7][x0] = s.Ca.x; bt.ra[8][x0] = Ge.x; bt.ra[9][x0] = Gi.x;
@@ -504,11 +527,11 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
     }
 }
 
-template <class R>
+template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(NetDev<R> n, BatchDev<R> bt, int q, int s0,
                                                                            int s1, RAStep<R> rc)
 {
-    interval_ra_x2_body(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
+    interval_ra_x2_body<R, kTrack>(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // Single build: draws every Poisson noise event of the trial for each

@@ -31,7 +31,8 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_append_num_synapses", "ug_append_replaced", "ug_write_jitter", "ug_write_spike_times",
             "ug_write_graph_state", "ug_create_growth_network", "ug_get_trial_stats", "ug_get_spikes", "ug_get_neuron_state",
             "ug_step_time", "ug_launch_count", "ug_set_kernel_timing", "ug_get_kernel_timing",
-            "ug_run_test_trial_noalloc", "ug_generate_topology", "ug_topology_get_info",
+            "ug_run_test_trial_noalloc", "ug_set_inhibition_tracking", "ug_get_inhibitory_conductance",
+            "ug_write_inhibition_tracking_state", "ug_generate_topology", "ug_topology_get_info",
             "ug_topology_get_coordinates", "ug_topology_get_connections", "ug_topology_get_training",
             "ug_topology_write_dir", "ug_topology_free", "ug_create_network_topology", "ug_calibrate_pipes"]
 
@@ -193,6 +194,9 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_kernel_timing.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.ug_run_test_trial_noalloc.argtypes = [vp, C.c_int32, C.c_uint32] + [C.c_void_p] * 6
     L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ug_set_inhibition_tracking.argtypes = [vp, C.c_int32, C.c_double]
+    L.ug_get_inhibitory_conductance.argtypes = [vp, C.c_int32, _f64p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    L.ug_write_inhibition_tracking_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
     L.ug_generate_topology.argtypes = [vp, C.POINTER(TopologyParams), C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                        C.c_int32, C.POINTER(vp)]
     L.ug_topology_get_info.argtypes = [vp, C.POINTER(TopologyInfo)]
@@ -357,6 +361,22 @@ class ResidentNetwork:
 
     def write_jitter(self, path: str):
         _check(self.engine.L.ug_write_jitter(self.engine.ctx, self.id, path.encode()))
+
+    def set_inhibition_tracking(self, resolution_ms: float):
+        """Every later growth trial records each HVC(RA) neuron's Ginh_d every resolution_ms
+        (trial_..._with_inhibition_tracking); 0 switches it off."""
+        _check(self.engine.L.ug_set_inhibition_tracking(self.engine.ctx, self.id, resolution_ms))
+
+    def inhibitory_conductance(self):
+        """The last growth trial's record, [n_ra][points], and the resolution in ms."""
+        L, n, res = self.engine.L, C.c_int32(0), C.c_double(0)
+        _check(L.ug_get_inhibitory_conductance(self.engine.ctx, self.id, None, C.byref(n), C.byref(res)))
+        out = np.zeros((self.net.n_ra, n.value))
+        _check(L.ug_get_inhibitory_conductance(self.engine.ctx, self.id, _ptr(out, _f64p), C.byref(n), C.byref(res)))
+        return out, res.value
+
+    def write_inhibition_tracking_state(self, directory: str, trial: int):
+        _check(self.engine.L.ug_write_inhibition_tracking_state(self.engine.ctx, self.id, directory.encode(), trial))
 
     def free(self):
         if self.id is not None:

@@ -310,6 +310,36 @@ def read_jitter(path):
     return r.take(F8, 8 * n).reshape(n, 8).copy(), trials
 
 
+def write_inhibitory_conductance(path, ginh, resolution):
+    """write_inhibitory_conductance (NetworkGrowthSimulator.cpp:17689-17709): N_RA, the number
+    of points, the resolution (ms), then each neuron's Ginh_d record."""
+    ginh = np.asarray(ginh, dtype=F8)
+    with open(path, "wb") as f:
+        _w(f, I4, [ginh.shape[0], ginh.shape[1]])
+        _w(f, F8, [resolution])
+        _w(f, F8, ginh.ravel())
+
+
+def read_inhibitory_conductance(path):
+    r = _Reader(path)
+    n, points = r.i(), r.i()
+    res = r.d()
+    return r.take(F8, n * points).reshape(n, points).copy(), res
+
+
+def inhibition_slots(step_times, resolution, points):
+    """The steps at which trial_..._with_inhibition_tracking records Ginh_d (:8432-8442):
+    slot p (1 <= p < points) at the first step whose time is at least p * resolution,
+    one slot per step at most.  step_times[s] is internal_time after step s (s >= 1)."""
+    slots, pos = {}, 1
+    for s in range(1, len(step_times)):
+        if step_times[s] >= pos * resolution:
+            if pos < points:
+                slots[s] = pos
+            pos += 1
+    return slots
+
+
 # -------------------------------------------------------------- parameter files
 SYNAPTIC_FIELDS = ["Nss", "A_P", "A_D", "T_0", "T_P", "T_D", "TAU_P", "TAU_D", "BETA", "BETA_SUPERSYNAPSE",
                    "ACTIVATION_THRESHOLD", "SUPERSYNAPSE_THRESHOLD", "WEIGHT_MAX"]
