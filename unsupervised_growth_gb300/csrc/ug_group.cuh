@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(kBlock) kl_growth_epilogue(const GroupMember<R
 {
     __shared__ GroupMember<R> M;
     for_items(members, items, *count, M,
-              [](const GroupMember<R>& m, int bx, int b) { g_epilogue_body(m.g, bx, b); });
+              [](const GroupMember<R>& m, int bx, int b) { g_epilogue_rows(m.g, b, bx * kBlock, kBlock); });
 }
 
 // items: (member, chunk, 0) over 256-neuron chunks; bad[member] is set on a bad value.

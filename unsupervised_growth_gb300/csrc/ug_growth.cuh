@@ -1019,26 +1019,53 @@ __global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n,
 }
 
 // potentiation_decay + update_all_synapses (:16346-16361, :16432-16443).
-__device__ __forceinline__ void g_epilogue_body(const GrowthDev& g, int bx, int b)
+// potentiation_decay (:16346-16361) then update_all_synapses (:16432-16443) for rows
+// row0 .. row0 + nrows - 1 of network b, one warp per row: lanes decay 32 weights at a time
+// (coalesced) and test whether update_synapse could change the pair.  The state machine
+// changes a pair only when its weight is on the other side of a threshold than its
+// active / super flag, so that test (without the row-state conditions, which only
+// restrict) finds every pair it acts on; lane 0 then runs it on those, in target order.
+// A row's decay and updates read no other row, so rows need no barrier between them.
+__device__ __forceinline__ void g_epilogue_rows(const GrowthDev& g, int b, int row0, int nrows)
 {
-    const int i = bx * kBlock + threadIdx.x;
-    if (i >= g.n) return;
+    const int lane = threadIdx.x & 31;
+    const int row_end = min(row0 + nrows, g.n);
     const SynParams& sp = g.sp;
-    double* Wr = g.W + ((size_t)b * g.n + i) * g.n;
-    for (int j = 0; j < g.n; ++j) {
-        double w = Wr[j];
-        if (w >= sp.SUPERSYNAPSE_THRESHOLD) w -= sp.BETA_SUPERSYNAPSE;
-        else w -= sp.BETA;
-        if (w < 0) w = 0;
-        Wr[j] = w;
+    for (int i = row0 + (int)(threadIdx.x >> 5); i < row_end; i += (int)(blockDim.x >> 5)) {
+        const size_t base = ((size_t)b * g.n + i) * g.n;
+        double* Wr = g.W + base;
+        const uint8_t* act = g.active + base;
+        const uint8_t* sup = g.super + base;
+        for (int j0 = 0; j0 < g.n; j0 += 32) {
+            const int j = j0 + lane;
+            bool change = false;
+            if (j < g.n) {
+                double w = Wr[j];
+                if (w >= sp.SUPERSYNAPSE_THRESHOLD) w -= sp.BETA_SUPERSYNAPSE;
+                else w -= sp.BETA;
+                if (w < 0) w = 0;
+                Wr[j] = w;
+                const bool a = act[j] != 0, su = sup[j] != 0;
+                change = (w >= sp.ACTIVATION_THRESHOLD) != a || (w >= sp.SUPERSYNAPSE_THRESHOLD) != su;
+            }
+            __syncwarp();   // the decayed weights are visible to lane 0
+            unsigned m = __ballot_sync(0xffffffffu, change);
+            if (lane == 0)
+                while (m) {
+                    const int k = __ffs(m) - 1;
+                    m &= m - 1;
+                    g_update_synapse(g, b, i, j0 + k);
+                }
+            __syncwarp();
+        }
     }
-    for (int j = 0; j < g.n; ++j) g_update_synapse(g, b, i, j);
 }
 
 template <class R>
 __global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
 {
-    g_epilogue_body(g, (int)blockIdx.x, (int)blockIdx.y);
+    const int rows = kBlock / 32;   // one row per warp
+    g_epilogue_rows(g, (int)blockIdx.y, (int)blockIdx.x * rows, rows);
 }
 
 // Start of a growth trial: no streams, no pre or post events

@@ -147,7 +147,7 @@ cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const Bat
 template <class R>
 cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc)
 {
-    const dim3 rows((g.n + kBlock - 1) / kBlock, g.B);
+    const dim3 rows((g.n + kBlock / 32 - 1) / (kBlock / 32), g.B);   // a warp per row
     UG_TIMED(lc, "k_growth_epilogue", (k_growth_epilogue<R><<<rows, kBlock, 0, lc.main>>>(g)));
     return cudaGetLastError();
 }
