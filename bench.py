@@ -310,10 +310,19 @@ def run_ours(args, rank, world, local_rank):
     return result
 
 
-def make_growth_network():
+# Fast-growing synaptic and maturation parameters (the growth parity tests' set): the
+# active and super topology change within a few trials, so single and double precision
+# can be compared on a topology that has grown.
+FAST_SYN = dict(Nss=2, A_P=20.0, A_D=20.0 / 1.05, T_0=0.0, T_P=10.0, T_D=10.0, TAU_P=30.0, TAU_D=30.0, BETA=0.2,
+                BETA_SUPERSYNAPSE=0.2, ACTIVATION_THRESHOLD=10.0, SUPERSYNAPSE_THRESHOLD=40.0, WEIGHT_MAX=160.0)
+FAST_MAT = dict(RATE_WINDOW_LONG=1000, E_REST_IMMATURE=-65.0, GCA_IMMATURE=25.0, DEATH_RATE_THRESHOLD=0.01)
+
+
+def make_growth_network(num_steps=NUM_STEPS, fast=False):
     from unsupervised_growth_gb300.network import synthetic_growth_network
+    extra = dict(syn=FAST_SYN, mat=FAST_MAT) if fast else {}
     return synthetic_growth_network(n_ra=N_RA, n_i=N_I, n_tr=10, seed=2, delays="lognormal", lognormal_mean=3.0,
-                                    lognormal_sigma=1.5, delay_cap=10.0)
+                                    lognormal_sigma=1.5, delay_cap=10.0, num_steps=num_steps, **extra)
 
 
 def run_growth(args, local_rank):
@@ -326,7 +335,7 @@ def run_growth(args, local_rank):
     from unsupervised_growth_gb300.engine import Engine
     B.build()
     torch.cuda.set_device(local_rank)
-    net = make_growth_network()
+    net = make_growth_network(num_steps=args.num_steps)
     eng = Engine(precision=32, device=local_rank)
     rn = eng.load_network(net)
     rn.run_growth_trials(0, args.warmup, True)
@@ -346,13 +355,14 @@ def run_growth(args, local_rank):
              "k_growth_epilogue", "k_trial_init", "k_noise_events", "k_growth_reset")
     kt = {k: eng.kernel_timing(k) for k in names}
     eng.set_kernel_timing(False)
-    result = {"metric": "growth trials/s (500 ms growth trials, 2000 RA + 550 I network, one network)",
+    trial_ms = (args.num_steps - 1) * 0.02
+    result = {"metric": f"growth trials/s ({trial_ms:g} ms growth trials, 2000 RA + 550 I network, one network)",
               "value": args.steps / wall, "unit": "trials/s", "n_gpus": 1, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True,
               "dtype": "f32 neurons, f64 weights", "data": "synthetic (seeded network and Philox noise)",
               "config": {"workload": "growth trials of one 2000 HVC-RA + 550 HVC-I sphere network, lognormal "
-                                     "delays mean 3 ms capped 10 ms, 10 training neurons"},
-              "neuron_steps_per_s": args.steps / wall * (N_RA + N_I) * (NUM_STEPS - 1),
+                                     "delays mean 3 ms capped 10 ms, 10 training neurons", "trial_ms": trial_ms},
+              "neuron_steps_per_s": args.steps / wall * (N_RA + N_I) * (args.num_steps - 1),
               "gpu_launches": launches, "clocks": clk.summary(),
               "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()}}
     if not args.skip_fp64:
@@ -641,7 +651,7 @@ def run_topology(args, local_rank):
     from unsupervised_growth_gb300 import build as B
     from unsupervised_growth_gb300.engine import Engine
     B.build()
-    net = make_growth_network()
+    net = make_growth_network(num_steps=args.num_steps, fast=args.fast_growth)
     e32, e64 = Engine(precision=32, device=local_rank), Engine(precision=64, device=local_rank)
     r32, r64 = e32.load_network(net), e64.load_network(net)
     first_div = {"super": None, "active": None}
@@ -675,7 +685,10 @@ def run_topology(args, local_rank):
            "n_gpus": 1, "steps": args.steps, "warmup": 0, "higher_is_better": True,
            "dtype": "f32 neurons, f64 weights vs f64", "data": "synthetic (seeded network and Philox noise)",
            "config": {"workload": "growth trials of one 2000 HVC-RA + 550 HVC-I sphere network, lognormal delays "
-                                  "mean 3 ms capped 10 ms, 10 training neurons"},
+                                  "mean 3 ms capped 10 ms, 10 training neurons"
+                                  + (", fast-growing synapses (A_P 20, thresholds 10/40, Nss 2)" if args.fast_growth
+                                     else ""),
+                      "trial_ms": (args.num_steps - 1) * 0.02},
            "first_divergent_trial": first_div, "supersynapses_at_end": sup,
            "max_weight_abs_error": worst_w, "max_weight_rel_error": worst_rel,
            "soma_spikes_fp64": spikes, "min_fraction_matched_within_1_step": min_match, "max_step_error": worst_step,
@@ -723,6 +736,10 @@ def main():
                          "of requests through the serving loop; topology: single vs double precision over "
                          "consecutive growth trials; create: network topology generation (createNetworkForGrowth)")
     ap.add_argument("--create-size", default="2000x550", help="create: HVC(RA) x HVC(I)")
+    ap.add_argument("--num-steps", type=int, default=NUM_STEPS,
+                    help="growth, topology: steps per trial + 1 (25000: 500 ms trials; profiling runs use fewer)")
+    ap.add_argument("--fast-growth", action="store_true",
+                    help="topology: fast-growing synaptic parameters, so that supersynapses form within a few trials")
     ap.add_argument("--members", type=int, default=64, help="uneven: networks in the group; serve: member slots")
     ap.add_argument("--requests", type=int, default=48, help="serve: requests in the stream")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")

@@ -1036,26 +1036,44 @@ __device__ __forceinline__ void g_epilogue_rows(const GrowthDev& g, int b, int r
         double* Wr = g.W + base;
         const uint8_t* act = g.active + base;
         const uint8_t* sup = g.super + base;
-        for (int j0 = 0; j0 < g.n; j0 += 32) {
-            const int j = j0 + lane;
-            bool change = false;
-            if (j < g.n) {
-                double w = Wr[j];
-                if (w >= sp.SUPERSYNAPSE_THRESHOLD) w -= sp.BETA_SUPERSYNAPSE;
-                else w -= sp.BETA;
-                if (w < 0) w = 0;
-                Wr[j] = w;
-                const bool a = act[j] != 0, su = sup[j] != 0;
-                change = (w >= sp.ACTIVATION_THRESHOLD) != a || (w >= sp.SUPERSYNAPSE_THRESHOLD) != su;
+        // 128 targets per pass, four independent loads per lane in flight
+        for (int j0 = 0; j0 < g.n; j0 += 128) {
+            double w[4];
+            uint8_t a[4], su[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int j = j0 + 32 * k + lane;
+                if (j < g.n) {
+                    w[k] = Wr[j];
+                    a[k] = act[j];
+                    su[k] = sup[j];
+                }
+            }
+            unsigned m[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int j = j0 + 32 * k + lane;
+                bool change = false;
+                if (j < g.n) {
+                    double x = w[k];
+                    if (x >= sp.SUPERSYNAPSE_THRESHOLD) x -= sp.BETA_SUPERSYNAPSE;
+                    else x -= sp.BETA;
+                    if (x < 0) x = 0;
+                    Wr[j] = x;
+                    change = (x >= sp.ACTIVATION_THRESHOLD) != (a[k] != 0) ||
+                             (x >= sp.SUPERSYNAPSE_THRESHOLD) != (su[k] != 0);
+                }
+                m[k] = __ballot_sync(0xffffffffu, change);
             }
             __syncwarp();   // the decayed weights are visible to lane 0
-            unsigned m = __ballot_sync(0xffffffffu, change);
             if (lane == 0)
-                while (m) {
-                    const int k = __ffs(m) - 1;
-                    m &= m - 1;
-                    g_update_synapse(g, b, i, j0 + k);
-                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k)
+                    while (m[k]) {
+                        const int b2 = __ffs(m[k]) - 1;
+                        m[k] &= m[k] - 1;
+                        g_update_synapse(g, b, i, j0 + 32 * k + b2);
+                    }
             __syncwarp();
         }
     }
