@@ -40,9 +40,9 @@ SEED = 3
 #   I : 12 stages x 63 ops + 376 ops of the DP8 tableau sums      = 1132 FP32 ops; 12 x (4 ex2 + 1 rcp) = 60 SFU
 FP32_RA, FP32_I = 488, 1132
 MUFU_RA, MUFU_I = 40, 60
-# DRAM bytes per launch of the dominant kernel from the committed ncu capture
-# (profiles/k_interval_integrators_128trials_full.md: 16.4 MB read, ~0 written at
-# 128 trials), scaled to a launch of BATCH trials: the state read grows with the trials.
+# DRAM bytes per launch of the dominant kernel from an ncu capture of the integrators
+# at 128 trials (16.4 MB read, ~0 written), scaled to a launch of BATCH trials: the state
+# read grows with the trials.
 DRAM_BYTES_RA_PER_TRIAL = 16.4e6 / 128
 CPU_SAMPLE_STEPS = 6000   # first 120 ms of a trial (includes the training kick at 100 ms)
 
