@@ -374,6 +374,13 @@ ug_status ug_topology_get_training(const ug_topology* t, int32_t which, int32_t*
  * training files into `network_dir`. */
 ug_status ug_topology_write_dir(const ug_topology* t, const char* network_dir);
 void ug_topology_free(ug_topology* t);
+/* new_chain_growth's set-up (as ug_create_growth_network) on a generated topology held in
+ * memory: no topology directory is written or read.  training_set 0 takes the clustered
+ * training neurons, 1 the random ones; network_parameters.cfg in out_dir (when given) holds
+ * the topology's parameters. */
+ug_status ug_create_growth_network_from_topology(ug_ctx* ctx, const ug_topology* topo, int32_t training_set,
+                                                 const char* config_file, const char* out_dir, int32_t num_steps,
+                                                 uint64_t seed, int32_t stream_id, int32_t* net_id);
 /* createNetworkForGrowth (c++/createNetworkForGrowth/main.cpp): reads the spatialParameters
  * of `config_file` and writes a generated topology into `network_dir`. */
 ug_status ug_create_network_topology(ug_ctx* ctx, const char* config_file, const char* network_dir, int32_t n_ra,

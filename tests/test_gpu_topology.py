@@ -133,3 +133,44 @@ def test_directory_and_chain_growth(eng, tmp_path):
     np.testing.assert_allclose(np.concatenate(D2), np.concatenate(L) * 0.01, rtol=1e-15)
     assert (np.concatenate(W2) <= 0.1).all() and (np.concatenate(W2) > 0).any()
     assert (grown / "weights_1.bin").exists()
+
+
+def test_growth_network_from_topology(tmp_path):
+    """new_chain_growth's set-up on a generated topology in memory gives the network that the
+    same set-up gives from the topology's directory: the same weights, delays, connections
+    and neuron state, and the same next growth trial."""
+    from tests.helpers import sorted_spikes
+    from tests.test_gpu_cli import SYN6
+    from tests.test_gpu_growth import MAT
+    from unsupervised_growth_gb300.engine import Engine
+    from unsupervised_growth_gb300.network import DEFAULT_NOISE
+    p = dict(A_RA2I=0.1, SIGMA_RA2I=85.0, B_I2RA=0.1, SIGMA_I2RA=85.0)   # exact at the files' six decimals
+    eng = Engine(precision=32)
+    t = eng.generate_topology(p, 120, 30, 8, seed=21)
+    d = tmp_path / "net"
+    d.mkdir()
+    t.write_dir(f"{d}/")
+    F.write_topology_cfg(str(d / "network_parameters.cfg"), "sphere", p["A_RA2I"], p["SIGMA_RA2I"], p["B_I2RA"],
+                         p["SIGMA_I2RA"])
+    gcfg = tmp_path / "growth_parameters.cfg"
+    F.write_growth_cfg(str(gcfg), SYN6, MAT, DEFAULT_NOISE, dict(Gei_max=0.25, Gie_max=0.1, delay_constant=1.0))
+    a = eng.create_growth_network_from_topology(t, 0, str(gcfg), seed=5)
+    b = eng.create_growth_network(f"{d}/", str(d / "training_neurons_clustered.bin"), str(gcfg), seed=5)
+    assert np.array_equal(a.weights(), b.weights()) and np.array_equal(a.delays(), b.delays())
+    for which in (0, 1):
+        for x, y in zip(a.connections(which), b.connections(which)):
+            assert np.array_equal(x, y)
+    pa, pb = a.neuron_props(), b.neuron_props()
+    for k in ("rest_potential", "gca", "mature", "maturation_scale"):
+        assert np.array_equal(pa[k], pb[k]), k
+    assert pa["mature"].sum() == 8
+    with pytest.raises(Exception):
+        eng.create_growth_network_from_topology(t, 2, str(gcfg))   # no such training set
+    a.run_growth_trials(0, 1, True)
+    b.run_growth_trials(0, 1, True)
+    for w in (0, 1, 2):
+        assert np.array_equal(sorted_spikes(*a.spikes(0, w)), sorted_spikes(*b.spikes(0, w))), w
+    assert np.array_equal(a.weights(), b.weights())
+    t.free()
+    a.free()
+    b.free()

@@ -862,36 +862,111 @@ double sphere_dist(const double* a, const double* b)
 
 }  // namespace
 
+namespace {
+
+// What new_chain_growth's set-up reads from a topology directory (read_network_topology,
+// NetworkGrowthSimulator.cpp:2628-2650) plus the training neurons.
+struct GrowthSetup {
+    int32_t nra = 0, ni = 0;
+    double model = 0.0;
+    std::vector<double> ra_xyz, i_xyz;   // 3 per neuron
+    Conn ri, ir;
+    std::vector<int32_t> training;       // sorted
+    Cfg t;                               // the topology parameters (network_parameters.cfg)
+};
+
+ug_status setup_growth_network(ug_ctx* ctx, GrowthSetup& su, const Cfg& g, const std::string& out_dir,
+                               int32_t num_steps, uint64_t seed, int32_t stream_id, int32_t* net_id);
+
+}  // namespace
+
 extern "C" ug_status ug_create_growth_network(ug_ctx* ctx, const char* network_dir, const char* training_file,
                                               const char* config_file, const char* out_dir_c, int32_t num_steps,
                                               uint64_t seed, int32_t stream_id, int32_t* net_id)
 {
     if (!ctx || !network_dir || !training_file || !config_file || !net_id) return ferr(UG_EINVAL, "null argument");
     const std::string dir(network_dir), out_dir(out_dir_c ? out_dir_c : "");
-    Cfg g, t;
+    Cfg g;
+    GrowthSetup su;
     UG_FTRY(parse_cfg(config_file, g));
-    UG_FTRY(parse_cfg(join(dir, "network_parameters.cfg"), t));
-    int32_t nra = 0, ni = 0;
+    UG_FTRY(parse_cfg(join(dir, "network_parameters.cfg"), su.t));
     {
         In in(join(dir, "num_neurons.bin"));
-        if (!in.ok() || !in.get(nra) || !in.get(ni) || nra <= 0 || ni < 0) return bad_file(in);
+        if (!in.ok() || !in.get(su.nra) || !in.get(su.ni) || su.nra <= 0 || su.ni < 0) return bad_file(in);
     }
-    std::vector<double> ra_xyz, i_xyz;
-    double model = 0.0, model_i = 0.0;
-    UG_FTRY(read_coords(join(dir, "RA_xy.bin"), nra, ra_xyz, model));
-    UG_FTRY(read_coords(join(dir, "I_xy.bin"), ni, i_xyz, model_i));
-    Conn ri, ir;
-    UG_FTRY(read_connections(join(dir, "RA_I_connections.bin"), nra, ri.off, ri.tgt, ri.w, ri.len, ri.d));
-    UG_FTRY(read_connections(join(dir, "I_RA_connections.bin"), ni, ir.off, ir.tgt, ir.w, ir.len, ir.d));
-    std::vector<int32_t> training;
+    double model_i = 0.0;
+    UG_FTRY(read_coords(join(dir, "RA_xy.bin"), su.nra, su.ra_xyz, su.model));
+    UG_FTRY(read_coords(join(dir, "I_xy.bin"), su.ni, su.i_xyz, model_i));
+    UG_FTRY(read_connections(join(dir, "RA_I_connections.bin"), su.nra, su.ri.off, su.ri.tgt, su.ri.w, su.ri.len,
+                             su.ri.d));
+    UG_FTRY(read_connections(join(dir, "I_RA_connections.bin"), su.ni, su.ir.off, su.ir.tgt, su.ir.w, su.ir.len,
+                             su.ir.d));
     {
         In in(training_file);
         int32_t k = 0;
-        if (!in.ok() || !in.get(k) || k < 0 || !in.get(training, (size_t)k)) return bad_file(in);
-        std::sort(training.begin(), training.end());
-        for (int32_t id : training)
-            if (id < 0 || id >= nra) return ferr(UG_EINVAL, "training neuron out of range");
+        if (!in.ok() || !in.get(k) || k < 0 || !in.get(su.training, (size_t)k)) return bad_file(in);
     }
+    return setup_growth_network(ctx, su, g, out_dir, num_steps, seed, stream_id, net_id);
+}
+
+extern "C" ug_status ug_create_growth_network_from_topology(ug_ctx* ctx, const ug_topology* topo, int32_t training_set,
+                                                            const char* config_file, const char* out_dir_c,
+                                                            int32_t num_steps, uint64_t seed, int32_t stream_id,
+                                                            int32_t* net_id)
+{
+    if (!ctx || !topo || !config_file || !net_id) return ferr(UG_EINVAL, "null argument");
+    if (training_set != 0 && training_set != 1) return ferr(UG_EINVAL, "training_set must be 0 (clustered) or 1 (random)");
+    Cfg g;
+    UG_FTRY(parse_cfg(config_file, g));
+    GrowthSetup su;
+    su.nra = topo->n_ra;
+    su.ni = topo->n_i;
+    su.model = topo->model;
+    su.ra_xyz = topo->ra_xyz;
+    su.i_xyz = topo->i_xyz;
+    su.ri.off = topo->ri_off;
+    su.ri.tgt = topo->ri_tgt;
+    su.ri.len = topo->ri_len;
+    su.ri.w.assign(topo->ri_tgt.size(), 0.0);
+    su.ri.d.assign(topo->ri_tgt.size(), 0.0);
+    su.ir.off = topo->ir_off;
+    su.ir.tgt = topo->ir_tgt;
+    su.ir.len = topo->ir_len;
+    su.ir.w.assign(topo->ir_tgt.size(), 0.0);
+    su.ir.d.assign(topo->ir_tgt.size(), 0.0);
+    su.training = training_set == 0 ? topo->clustered : topo->random_set;
+    // the topology parameters as network_parameters.cfg would hold them, at full precision
+    auto& sp = su.t.groups["spatialParameters"];
+    sp["arrangement"] = topo->params.arrangement == UG_ARRANGEMENT_SQUARE ? "square" : "sphere";
+    const double vals[4] = {topo->params.A_RA2I, topo->params.SIGMA_RA2I, topo->params.B_I2RA, topo->params.SIGMA_I2RA};
+    const char* keys[4] = {"A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA"};
+    for (int k = 0; k < 4; ++k) {
+        char b[64];
+        std::snprintf(b, sizeof(b), "%.17g", vals[k]);
+        sp[keys[k]] = b;
+    }
+    return setup_growth_network(ctx, su, g, out_dir_c ? out_dir_c : "", num_steps, seed, stream_id, net_id);
+}
+
+namespace {
+
+// The rest of new_chain_growth's set-up (NetworkGrowthSimulator.cpp:1865-1940) on what
+// was read: delays from the lengths, the RA<->I weights redrawn, the training neurons made
+// mature, the set-up files written into out_dir (when given), and the network loaded.
+ug_status setup_growth_network(ug_ctx* ctx, GrowthSetup& su, const Cfg& g, const std::string& out_dir,
+                               int32_t num_steps, uint64_t seed, int32_t stream_id, int32_t* net_id)
+{
+    const int32_t nra = su.nra, ni = su.ni;
+    const double model = su.model;
+    std::vector<double>& ra_xyz = su.ra_xyz;
+    std::vector<double>& i_xyz = su.i_xyz;
+    Conn& ri = su.ri;
+    Conn& ir = su.ir;
+    const Cfg& t = su.t;
+    std::vector<int32_t>& training = su.training;
+    std::sort(training.begin(), training.end());
+    for (int32_t id : training)
+        if (id < 0 || id >= nra) return ferr(UG_EINVAL, "training neuron out of range");
     double dc = 0.0, gei = 0.0, gie = 0.0;
     g.num("connectionParameters", "delay_constant", dc);
     g.num("connectionParameters", "Gei_max", gei);
@@ -1004,6 +1079,8 @@ extern "C" ug_status ug_create_growth_network(ug_ctx* ctx, const char* network_d
     d.ra_xyz = ra_xyz.data(); d.i_xyz = i_xyz.data();
     return ug_load_network(ctx, &d, net_id);
 }
+
+}  // namespace
 
 // ---------------------------------------------------------------- generated topologies
 

@@ -34,7 +34,8 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_run_test_trial_noalloc", "ug_set_inhibition_tracking", "ug_get_inhibitory_conductance",
             "ug_write_inhibition_tracking_state", "ug_generate_topology", "ug_topology_get_info",
             "ug_topology_get_coordinates", "ug_topology_get_connections", "ug_topology_get_training",
-            "ug_topology_write_dir", "ug_topology_free", "ug_create_network_topology", "ug_calibrate_pipes"]
+            "ug_topology_write_dir", "ug_topology_free", "ug_create_growth_network_from_topology",
+            "ug_create_network_topology", "ug_calibrate_pipes"]
 
 
 class UGError(RuntimeError):
@@ -208,6 +209,8 @@ def load_library(path: str = LIB_PATH):
     L.ug_topology_free.restype = None
     L.ug_create_network_topology.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_uint64,
                                              C.POINTER(TopologyInfo)]
+    L.ug_create_growth_network_from_topology.argtypes = [vp, vp, C.c_int32, C.c_char_p, C.c_char_p, C.c_int32,
+                                                         C.c_uint64, C.c_int32, _i32p]
     for name in EXPORTED:
         if name not in ("ug_last_error", "ug_destroy", "ug_topology_free"):
             getattr(L, name).restype = C.c_int
@@ -500,6 +503,31 @@ class Engine:
         _check(self.L.ug_create_network_topology(self.ctx, config_file.encode(), network_dir.encode(), n_ra, n_i,
                                                  n_tr, seed, C.byref(x)))
         return {k: getattr(x, k) for k, _ in TopologyInfo._fields_}
+
+    def _resident(self, nid: int, seed: int, stream_id: int) -> ResidentNetwork:
+        x = NetworkInfo()
+        _check(self.L.ug_get_network_info(self.ctx, nid, C.byref(x)))
+        net = Network(n_ra=x.n_ra, n_i=x.n_i, seed=seed, num_steps=x.num_steps, net_id=stream_id)
+        return ResidentNetwork(self, net, nid)
+
+    def create_growth_network(self, network_dir: str, training_file: str, config_file: str, out_dir: str = "",
+                              num_steps: int = 0, seed: int = 15000, stream_id: int = 0) -> ResidentNetwork:
+        """new_chain_growth's set-up from a topology directory (ug_create_growth_network)."""
+        nid = C.c_int32(-1)
+        _check(self.L.ug_create_growth_network(self.ctx, network_dir.encode(), training_file.encode(),
+                                               config_file.encode(), out_dir.encode(), num_steps, seed, stream_id,
+                                               C.byref(nid)))
+        return self._resident(nid.value, seed, stream_id)
+
+    def create_growth_network_from_topology(self, topo: "Topology", training_set: int, config_file: str,
+                                            out_dir: str = "", num_steps: int = 0, seed: int = 15000,
+                                            stream_id: int = 0) -> ResidentNetwork:
+        """The same set-up on a generated topology in memory (training_set 0: clustered, 1: random)."""
+        nid = C.c_int32(-1)
+        _check(self.L.ug_create_growth_network_from_topology(self.ctx, topo.h, training_set, config_file.encode(),
+                                                             out_dir.encode(), num_steps, seed, stream_id,
+                                                             C.byref(nid)))
+        return self._resident(nid.value, seed, stream_id)
 
     def load_network(self, net: Network) -> ResidentNetwork:
         d, keep = make_desc(net)
