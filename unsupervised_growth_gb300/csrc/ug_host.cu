@@ -967,7 +967,9 @@ ug_status NetImpl<R>::set_inhibition_tracking(double resolution, cudaStream_t st
         ginh_points_ = 0;
         return UG_OK;
     }
-    const int points = (int)(h.num_steps * kTimestep / resolution);
+    const double np = h.num_steps * kTimestep / resolution;
+    if (!(np < 1e8)) return fail(UG_EINVAL, "the resolution is too fine (more than 1e8 points per neuron)");
+    const int points = (int)np;
     if (points < 1) return fail(UG_EINVAL, "the resolution is longer than the trial");
     std::vector<int> slot(h.num_steps, -1);
     int pos = 1;
