@@ -1041,7 +1041,6 @@ ug_status setup_growth_network(ug_ctx* ctx, GrowthSetup& su, const Cfg& g, const
     d.num_steps = num_steps > 0 ? num_steps : 25000;
     d.net_id = stream_id;
     d.seed = seed;
-    Cfg none;
     auto num = [](const Cfg& c, const char* grp, const char* key) {
         double v = 0.0;
         c.num(grp, key, v);
