@@ -135,7 +135,7 @@ class ClockSampler:
 def _fp64_plain(net, device, trial, rn32):
     """Times one trial of the plain double-precision path (no batching, no graph)
     and compares the single build's spikes of the same trial with it."""
-    from tests.helpers import match_within, sorted_spikes
+    from unsupervised_growth_gb300.compare import match_within, sorted_spikes
     from unsupervised_growth_gb300.engine import Engine
     eng64 = Engine(precision=64, device=device, use_graphs=False)
     rn64 = eng64.load_network(net)
@@ -647,7 +647,7 @@ def run_topology(args, local_rank):
     differs, if any.  A step is one growth trial of both builds."""
     import numpy as np
 
-    from tests.helpers import match_within, sorted_spikes
+    from unsupervised_growth_gb300.compare import match_within, sorted_spikes
     from unsupervised_growth_gb300 import build as B
     from unsupervised_growth_gb300.engine import Engine
     B.build()

@@ -52,11 +52,33 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-def build_ref(ref_dir: str = "/root/reference/c++") -> str | None:
+def reference_dir() -> str:
+    """The reference's c++/ directory: UG_REFERENCE_DIR, else the mounted copy."""
+    return os.environ.get("UG_REFERENCE_DIR", "/root/reference/c++")
+
+
+def build_ref(ref_dir: str | None = None) -> str | None:
+    ref_dir = ref_dir or reference_dir()
     if not os.path.isdir(ref_dir):
         return None
     subprocess.run(["make", "-s", "ref", f"REF_DIR={ref_dir}"], cwd=HERE, check=True)
     return REF_PATH
+
+
+REF_SIM_PATHS = {"O2": os.path.join(HERE, "_ref", "librefsim.so"),
+                 "O0": os.path.join(HERE, "_ref", "librefsim_O0.so")}
+
+
+def build_ref_sim(ref_dir: str | None = None) -> bool:
+    """Compile the reference's own simulator (NetworkGrowthSimulator.cpp) against the
+    project-written MPI / Boost / libconfig stand-ins, at the shipped flags and at -O2.
+    Returns False where the reference tree is absent."""
+    ref_dir = ref_dir or reference_dir()
+    if not os.path.isdir(ref_dir):
+        return False
+    subprocess.run(["make", "-s", "-j2", "refsim", f"REF_DIR={ref_dir}"], cwd=HERE, check=True,
+                   stderr=subprocess.DEVNULL)
+    return True
 
 
 _P = C.POINTER
@@ -144,6 +166,43 @@ def ref_lib():
         R.ref_i_single.argtypes = lib()._single_i
         _ref = R
     return _ref
+
+
+_ref_sim = {}
+
+
+def ref_sim_lib(opt: str = "O2"):
+    """The reference's own simulator class behind the oracle's C interface (prefix
+    refsim_), or None where it was not built."""
+    if opt in _ref_sim:
+        return _ref_sim[opt]
+    path = REF_SIM_PATHS[opt]
+    if not os.path.exists(path):
+        return None
+    R = C.CDLL(path)
+    O = lib()
+    for fn in ("new", "free", "set_params", "set_seed", "set_num_steps", "set_ra2i", "set_i2ra", "set_rara",
+               "set_synapse_lists", "set_neuron_props", "set_training", "set_coordinates", "set_activity_history",
+               "run_trial", "after_growth_trial", "get_spikes", "get_weights", "get_delays", "get_list",
+               "get_neuron_props", "get_connections", "get_coordinates", "get_replaced"):
+        src, dst = getattr(O, "ugo_" + fn), getattr(R, "refsim_" + fn)
+        dst.argtypes = src.argtypes
+        dst.restype = src.restype
+    R.refsim_set_num_steps.restype = C.c_int32
+    _ref_sim[opt] = R
+    return R
+
+
+class _Prefixed:
+    """Presents the refsim_* functions under the oracle's ugo_* names."""
+
+    def __init__(self, L):
+        self._L = L
+
+    def __getattr__(self, name):
+        if not name.startswith("ugo_"):
+            raise AttributeError(name)
+        return getattr(self._L, "refsim_" + name[4:])
 
 
 def philox(ctr, key):
@@ -239,9 +298,9 @@ def i_single(n_steps, seed=1, trial=0, neuron=0, kicks=None, use_ref=False):
 class OracleNet:
     """One network held by the CPU restatement; mirrors the simulator's state."""
 
-    def __init__(self, net):
+    def __init__(self, net, L=None):
         """net: a unsupervised_growth_gb300.network.Network-like object (numpy arrays)."""
-        self.L = lib()
+        self.L = L if L is not None else lib()
         self.n_ra, self.n_i = net.n_ra, net.n_i
         self.h = self.L.ugo_new(self.n_ra, self.n_i)
         self.window = int(net.mat["RATE_WINDOW_LONG"])
@@ -378,3 +437,38 @@ class OracleNet:
         out = np.zeros(n, dtype=np.int32)
         self.L.ugo_get_replaced(self.h, _ptr(out, _i32p), n)
         return out
+
+
+class RefSimNet(OracleNet):
+    """The same network held by the reference's own simulator class
+    (NetworkGrowthSimulator, compiled from the reference tree into _ref/), driven
+    through the harness in ref_harness/sim_harness.cpp.  Same methods as
+    OracleNet except the trace, delivery-log and inhibition hooks, which exist
+    only in the restatement."""
+
+    def __init__(self, net, opt: str = "O2"):
+        R = ref_sim_lib(opt)
+        if R is None:
+            raise RuntimeError("the reference simulator is not built (oracle/Makefile target refsim)")
+        super().__init__(net, L=_Prefixed(R))
+        if R.refsim_set_num_steps(self.h, int(net.num_steps)) != 0:
+            raise ValueError("the reference's trial is 25000 steps; the network asks for %d" % net.num_steps)
+
+    @classmethod
+    def from_dir(cls, directory: str, trial: int, seed: int, net_id: int = 0, opt: str = "O2"):
+        """A network read by the reference's own read_network_state from a state
+        directory (the files of unsupervised_growth_gb300.files.write_network_state_dir)."""
+        R = ref_sim_lib(opt)
+        if R is None:
+            raise RuntimeError("the reference simulator is not built (oracle/Makefile target refsim)")
+        R.refsim_load_dir.restype = C.c_void_p
+        R.refsim_load_dir.argtypes = [C.c_char_p, C.c_int32]
+        R.refsim_sizes.argtypes = [C.c_void_p, _i32p, _i32p]
+        self = cls.__new__(cls)
+        self.L = _Prefixed(R)
+        self.h = R.refsim_load_dir(directory.encode(), int(trial))
+        n_ra, n_i = C.c_int32(), C.c_int32()
+        R.refsim_sizes(self.h, C.byref(n_ra), C.byref(n_i))
+        self.n_ra, self.n_i = n_ra.value, n_i.value
+        R.refsim_set_seed(self.h, int(seed), int(net_id))
+        return self

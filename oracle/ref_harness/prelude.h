@@ -5,4 +5,6 @@
 #include <vector>
 #include <functional>
 #include <iostream>
+#include <numeric>
+#include <algorithm>
 using std::isnan;

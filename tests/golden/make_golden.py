@@ -34,7 +34,7 @@ SCENARIOS = [
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/c++"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else O.reference_dir()
     if O.build_ref(ref_dir) is None:
         raise SystemExit(f"reference tree {ref_dir} not found")
     out = {}

@@ -1,7 +1,13 @@
 """Shared helpers of the parity tests: small seeded networks and comparisons."""
 import numpy as np
 
+from unsupervised_growth_gb300.compare import match_within, sorted_spikes  # noqa: F401  (re-exported)
 from unsupervised_growth_gb300.network import synthetic_chain_network, synthetic_growth_network
+
+# Fast-growing synapses: supersynapses form within a few trials on a 40/14 network.
+FAST_SYN = dict(Nss=2, A_P=20.0, A_D=20.0 / 1.05, T_0=0.0, T_P=10.0, T_D=10.0, TAU_P=30.0, TAU_D=30.0, BETA=0.2,
+                BETA_SUPERSYNAPSE=0.2, ACTIVATION_THRESHOLD=10.0, SUPERSYNAPSE_THRESHOLD=40.0, WEIGHT_MAX=160.0)
+FAST_MAT = dict(RATE_WINDOW_LONG=1000, E_REST_IMMATURE=-65.0, GCA_IMMATURE=25.0, DEATH_RATE_THRESHOLD=0.01)
 
 
 def small_chain(seed=5, n_ra=60, n_i=20, groups=5, group=10, weight=500.0, num_steps=25000, delay_cap=2.0, **kw):
@@ -13,33 +19,18 @@ def small_growth(seed=7, n_ra=40, n_i=14, n_tr=6, num_steps=25000, **kw):
     return synthetic_growth_network(n_ra=n_ra, n_i=n_i, n_tr=n_tr, seed=seed, num_steps=num_steps, **kw)
 
 
-def sorted_spikes(neuron, step):
-    order = np.lexsort((step, neuron))
-    return np.stack([neuron[order], step[order]], axis=1)
+def growth_net(seed=7, replace_ids=(), syn=None):
+    """The 40/14 fast-growth network of the growth parity tests; neurons in replace_ids
+    are made older than the 1000-trial robustness window, so silence replaces them."""
+    net = small_growth(seed=seed, n_ra=40, n_i=14, n_tr=8, syn=syn or FAST_SYN, mat=FAST_MAT, delays="uniform",
+                       delay_width=2.0)
+    net.training_spread = np.linspace(0.0, 15.0, len(net.training))
+    for r in replace_ids:
+        net.trials_after_replacement[r] = 1001
+    net.trials_after_replacement[net.training] = 0
+    return net
 
 
 def oracle_trial_spikes(onet, which):
     n, s = onet.spikes(which)
     return sorted_spikes(n, s)
-
-
-def match_within(a, b, tol_steps=1):
-    """Fraction of spikes of a matched to a spike of b of the same neuron within tol_steps (greedy)."""
-    if len(a) == 0 and len(b) == 0:
-        return 1.0, 0
-    matched = 0
-    worst = 0
-    bi = {}
-    for n, s in b:
-        bi.setdefault(int(n), []).append(int(s))
-    for n, s in a:
-        cand = bi.get(int(n), [])
-        best = None
-        for k, t in enumerate(cand):
-            if abs(t - int(s)) <= tol_steps and (best is None or abs(t - int(s)) < abs(cand[best] - int(s))):
-                best = k
-        if best is not None:
-            worst = max(worst, abs(cand[best] - int(s)))
-            cand.pop(best)
-            matched += 1
-    return matched / max(len(a), len(b)), worst

@@ -8,9 +8,10 @@ import re
 import numpy as np
 import pytest
 
+from oracle.oracle import reference_dir
 from unsupervised_growth_gb300 import files as F
 
-REF = "/root/reference/python_scripts/reading.py"
+REF = os.path.join(os.path.dirname(reference_dir().rstrip("/")), "python_scripts", "reading.py")
 
 
 def same(got, want):

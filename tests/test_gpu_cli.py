@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from tests.helpers import small_growth
-from tests.test_gpu_growth import MAT
+from tests.helpers import FAST_MAT as MAT
 from unsupervised_growth_gb300 import build as B
 from unsupervised_growth_gb300 import files as F
 

@@ -13,7 +13,7 @@ import pytest
 
 from tests.helpers import small_chain
 from tests.test_gpu_group import _assert_same, _state
-from tests.test_gpu_growth import growth_net
+from tests.helpers import growth_net
 from unsupervised_growth_gb300.engine import Engine, UGError
 
 pytestmark = pytest.mark.gpu

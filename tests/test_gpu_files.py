@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 from tests.helpers import small_chain, small_growth, sorted_spikes
-from tests.test_gpu_growth import MAT, SYN
+from tests.helpers import FAST_MAT as MAT, FAST_SYN as SYN
 from unsupervised_growth_gb300 import files as F
 
 pytestmark = pytest.mark.gpu

@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from tests.helpers import small_chain, small_growth
-from tests.test_gpu_growth import MAT, SYN, growth_net
+from tests.helpers import FAST_MAT as MAT, FAST_SYN as SYN, growth_net
 
 pytestmark = pytest.mark.gpu
 

@@ -12,23 +12,12 @@ import numpy as np
 import pytest
 
 from oracle.oracle import OracleNet
-from tests.helpers import match_within, oracle_trial_spikes, small_growth, sorted_spikes
+from tests.helpers import FAST_MAT as MAT, FAST_SYN as SYN, growth_net, match_within, oracle_trial_spikes, \
+    sorted_spikes  # noqa: F401
 
 pytestmark = pytest.mark.gpu
 
-SYN = dict(Nss=2, A_P=20.0, A_D=20.0 / 1.05, T_0=0.0, T_P=10.0, T_D=10.0, TAU_P=30.0, TAU_D=30.0, BETA=0.2,
-           BETA_SUPERSYNAPSE=0.2, ACTIVATION_THRESHOLD=10.0, SUPERSYNAPSE_THRESHOLD=40.0, WEIGHT_MAX=160.0)
-MAT = dict(RATE_WINDOW_LONG=1000, E_REST_IMMATURE=-65.0, GCA_IMMATURE=25.0, DEATH_RATE_THRESHOLD=0.01)
 TRIALS = 4
-
-
-def growth_net(seed=7, replace_ids=()):
-    net = small_growth(seed=seed, n_ra=40, n_i=14, n_tr=8, syn=SYN, mat=MAT, delays="uniform", delay_width=2.0)
-    net.training_spread = np.linspace(0.0, 15.0, len(net.training))
-    for r in replace_ids:
-        net.trials_after_replacement[r] = 1001   # silent for more than the 1000-trial window
-    net.trials_after_replacement[net.training] = 0
-    return net
 
 
 def _same_lists(a, b):

@@ -10,7 +10,7 @@ import pytest
 
 from oracle.oracle import OracleNet
 from tests.helpers import oracle_trial_spikes, small_growth, sorted_spikes
-from tests.test_gpu_growth import MAT, SYN
+from tests.helpers import FAST_MAT as MAT, FAST_SYN as SYN
 
 pytestmark = pytest.mark.gpu
 

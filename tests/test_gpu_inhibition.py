@@ -14,7 +14,7 @@ import pytest
 
 from oracle.oracle import OracleNet
 from tests.test_gpu_cli import topology  # noqa: F401  (the program test's network directory)
-from tests.test_gpu_growth import growth_net
+from tests.helpers import growth_net
 from unsupervised_growth_gb300 import files as F
 
 pytestmark = pytest.mark.gpu

@@ -12,7 +12,7 @@ import pytest
 
 from tests.helpers import small_chain, small_growth
 from tests.test_gpu_group import _assert_same, _state
-from tests.test_gpu_growth import MAT, SYN, growth_net
+from tests.helpers import FAST_MAT as MAT, FAST_SYN as SYN, growth_net
 
 pytestmark = pytest.mark.gpu
 

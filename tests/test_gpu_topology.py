@@ -88,7 +88,7 @@ def test_directory_and_chain_growth(eng, tmp_path):
     then grows the generated network (network_parameters.cfg copied in, as the reference's
     chainGrowth reads it from the network directory)."""
     from tests.test_gpu_cli import SYN6
-    from tests.test_gpu_growth import MAT
+    from tests.helpers import FAST_MAT as MAT
     from unsupervised_growth_gb300.network import DEFAULT_NOISE
     cfg = tmp_path / "network_parameters.cfg"
     F.write_topology_cfg(str(cfg), "sphere", P["A_RA2I"], P["SIGMA_RA2I"], P["B_I2RA"], P["SIGMA_I2RA"])
@@ -141,7 +141,7 @@ def test_growth_network_from_topology(tmp_path):
     and neuron state, and the same next growth trial."""
     from tests.helpers import sorted_spikes
     from tests.test_gpu_cli import SYN6
-    from tests.test_gpu_growth import MAT
+    from tests.helpers import FAST_MAT as MAT
     from unsupervised_growth_gb300.engine import Engine
     from unsupervised_growth_gb300.network import DEFAULT_NOISE
     p = dict(A_RA2I=0.1, SIGMA_RA2I=85.0, B_I2RA=0.1, SIGMA_I2RA=85.0)   # exact at the files' six decimals

@@ -1,0 +1,147 @@
+"""The oracle's trial orchestration pinned to the reference's own simulator.
+
+oracle/ug_oracle.cpp restates the per-trial path; here it is checked against
+the reference's NetworkGrowthSimulator class itself (c++/src/NetworkGrowthSimulator.cpp,
+compiled unmodified by oracle/Makefile target `refsim` against project-written
+stand-ins for MPI, two Boost containers and libconfig++), driven through
+oracle/ref_harness/sim_harness.cpp with the same noise streams.  Every
+comparison is exact: spikes at the same step, the same weight bits, the same
+ordered synapse lists, maturation state, replaced neurons and resampled
+positions, connections and delays.
+
+Covered: test trials (trial_no_stdp_fixedSpread, :12747-13117), growth trials
+with their per-trial tail (trial_1stSoma_pre_1stSoma_post_delays_fixedSpread,
+:8839-9571; chain_growth :5841-5875) on the fast-growth set where supersynapses
+form and rows saturate and remodel, replacement of silent neurons (:15757-15881,
+:157-220, :528-618), the 300/100 growth network with the STDP parameters of the
+config-1 workload (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold 0.035,
+Nss 3), a state directory read by the reference's own read_network_state
+(:1943-2020) through its libconfig readers, and the reference built with its
+shipped flags (-g, no optimisation) against the -O2 build.
+
+The reference tree is needed to build the simulator; where it is absent these
+tests are skipped (the committed fixtures of tests/golden pin the neuron
+classes there).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle.oracle import OracleNet, RefSimNet
+from tests.helpers import growth_net, oracle_trial_spikes, small_chain
+from unsupervised_growth_gb300 import files as F
+from unsupervised_growth_gb300.network import synthetic_growth_network
+
+
+@pytest.fixture(scope="module", autouse=True)
+def reference_sim():
+    if not O.build_ref_sim():
+        pytest.skip("reference tree not present: the simulator cannot be built")
+    assert O.ref_sim_lib("O2") is not None and O.ref_sim_lib("O0") is not None
+
+
+def same_spikes(a, b):
+    return all(np.array_equal(oracle_trial_spikes(a, w), oracle_trial_spikes(b, w)) for w in (0, 1, 2))
+
+
+def assert_same_state(o, r, t):
+    for w in (0, 1, 2):
+        assert np.array_equal(oracle_trial_spikes(o, w), oracle_trial_spikes(r, w)), (t, w)
+    assert np.array_equal(o.weights(), r.weights()), t          # bit for bit
+    assert o.synapse_list(0) == r.synapse_list(0), t            # ordered lists
+    assert o.synapse_list(1) == r.synapse_list(1), t
+    po, pr = o.neuron_props(), r.neuron_props()
+    for k in po:
+        assert np.array_equal(po[k], pr[k]), (t, k)
+
+
+def test_test_trials_match_reference():
+    net = small_chain()
+    o, r = OracleNet(net), RefSimNet(net)
+    for t in (0, 1):
+        assert o.run_trial(False, t) == 0
+        assert r.run_trial(False, t) == 0
+        assert same_spikes(o, r), t
+    n_soma = len(o.spikes(0)[0])
+    assert n_soma > 100   # the chain propagated
+
+
+def test_test_trials_lognormal_delays_match_reference():
+    """Log-normal delays up to 10 ms (the config-3 delay law) on a 60/20 chain."""
+    net = small_chain(seed=8, delays="lognormal", delay_cap=10.0)
+    o, r = OracleNet(net), RefSimNet(net)
+    assert o.run_trial(False, 3) == 0 and r.run_trial(False, 3) == 0
+    assert same_spikes(o, r)
+
+
+def test_growth_trials_match_reference():
+    net = growth_net()
+    o, r = OracleNet(net), RefSimNet(net)
+    for t in range(4):
+        assert o.run_trial(True, t) == 0
+        assert r.run_trial(True, t) == 0
+        assert o.after_growth_trial(t) == r.after_growth_trial(t) == 0
+        assert_same_state(o, r, t)
+    assert sum(map(len, o.synapse_list(1))) > 0             # supersynapses formed
+    assert o.neuron_props()["remodeled"].sum() > 0          # saturated rows were remodeled
+
+
+def test_replacement_matches_reference():
+    probe = growth_net(seed=11)
+    silent = [i for i in range(probe.n_ra) if i not in set(probe.training.tolist())][:3]
+    net = growth_net(seed=11, replace_ids=silent)
+    o, r = OracleNet(net), RefSimNet(net)
+    for t in range(2):
+        assert o.run_trial(True, t) == 0 and r.run_trial(True, t) == 0
+        assert o.after_growth_trial(t) == r.after_growth_trial(t)
+        assert np.array_equal(o.replaced(), r.replaced()), t
+        assert_same_state(o, r, t)
+        assert np.array_equal(o.delays(), r.delays()), t
+        for which in (0, 1):
+            for x, y in zip(o.connections(which), r.connections(which)):
+                assert np.array_equal(x, y), (t, which)
+        for x, y in zip(o.coordinates(), r.coordinates()):
+            assert np.array_equal(x, y), t
+        if t == 0:
+            assert sorted(o.replaced().tolist()) == sorted(silent)
+
+
+def test_config1_growth_matches_reference():
+    """300 HVC(RA) / 100 HVC(I), uniform 0-2 ms delays, the config-1 STDP set, two trials."""
+    net = synthetic_growth_network(n_ra=300, n_i=100, n_tr=10, seed=1)
+    assert net.syn["Nss"] == 3 and net.syn["SUPERSYNAPSE_THRESHOLD"] == 0.035
+    assert abs(net.syn["A_P"] - 1.05 * net.syn["A_D"]) < 1e-15 and net.syn["TAU_P"] == net.syn["TAU_D"] == 30.0
+    o, r = OracleNet(net), RefSimNet(net)
+    for t in range(2):
+        assert o.run_trial(True, t) == 0 and r.run_trial(True, t) == 0
+        o.after_growth_trial(t)
+        r.after_growth_trial(t)
+        assert_same_state(o, r, t)
+    assert (o.weights() > 0).sum() > 1000   # STDP changed many weights
+
+
+def test_state_directory_read_by_reference(tmp_path):
+    """The directory written by files.write_network_state_dir, read by the reference's
+    read_network_state and its libconfig readers, gives the network the oracle holds
+    from the arrays: the same next growth trial.  The parameters are written with six
+    decimals, so the network uses values that six decimals hold exactly."""
+    syn = dict(growth_net().syn, A_D=19.047619)
+    net = growth_net(seed=5, syn=syn)
+    net.training_spread = np.array([0.0, 2.5, 5.0, 7.5, 10.0, 12.5, 15.0, 17.5])
+    F.write_network_state_dir(str(tmp_path), net, trial=0)
+    o = OracleNet(net)
+    r = RefSimNet.from_dir(str(tmp_path), 0, seed=net.seed, net_id=net.net_id)
+    assert (r.n_ra, r.n_i) == (net.n_ra, net.n_i)
+    for t in range(2):
+        assert o.run_trial(True, t) == 0 and r.run_trial(True, t) == 0
+        o.after_growth_trial(t)
+        r.after_growth_trial(t)
+        assert_same_state(o, r, t)
+
+
+def test_shipped_flags_build_agrees():
+    """The reference built as shipped (-g, no optimisation) gives the -O2 build's results."""
+    net = small_chain(seed=6)
+    a, b = RefSimNet(net, opt="O0"), RefSimNet(net, opt="O2")
+    assert a.run_trial(False, 2) == 0 and b.run_trial(False, 2) == 0
+    assert same_spikes(a, b)

@@ -433,3 +433,38 @@ def state_paths(directory: str, trial: int) -> dict:
                 remodeled=j(f"remodeled_indicators{e}.bin"), training_spread=j("training_spread.bin"),
                 training=j("training_neurons.bin"), num_neurons=j("num_neurons.bin"),
                 topology_cfg=j("network_parameters.cfg"), growth_cfg=j("growth_parameters.cfg"))
+
+
+def write_network_state_dir(directory: str, net, trial: int = 0, arrangement: str = "sphere"):
+    """Every file read_network_state reads (:1943-2020) for a Network-like object
+    (unsupervised_growth_gb300.network.Network): the state at `trial`, the
+    coordinates, training set and sizes, and both parameter files.  Parameter
+    files keep six decimals, as the reference writes them."""
+    os.makedirs(directory, exist_ok=True)
+    p = state_paths(directory, trial)
+    n_ra, n_i = int(net.n_ra), int(net.n_i)
+    md = float(net.conn["model_interneuron_distance"])
+
+    def rows(off, vals):
+        return [np.asarray(vals[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
+
+    write_coordinates(p["RA_xy"], net.ra_xyz, md)
+    write_coordinates(p["I_xy"], net.i_xyz, md)
+    for key, off, tgt, w, ln, d in (("RA_I", net.ra2i_off, net.ra2i_tgt, net.ra2i_w, net.ra2i_len, net.ra2i_d),
+                                    ("I_RA", net.i2ra_off, net.i2ra_tgt, net.i2ra_w, net.i2ra_len, net.i2ra_d)):
+        write_connections(p[key], [r.tolist() for r in rows(off, tgt)], rows(off, w), rows(off, ln), rows(off, d))
+    write_axonal_delays(p["delays_RA2I"], rows(net.ra2i_off, net.ra2i_d), trial)
+    write_axonal_delays(p["delays_I2RA"], rows(net.i2ra_off, net.i2ra_d), trial)
+    write_axonal_delays(p["delays_RA2RA"], list(np.asarray(net.d_rara)), trial)
+    write_weights(p["weights"], net.w_rara, trial)
+    write_synapse_lists(p["active"], net.lists("active"), trial)
+    write_synapse_lists(p["super"], net.lists("super"), trial)
+    write_maturation_properties(p["maturation"], net.mature, net.maturation_scale, net.rest_potential, net.gca, trial)
+    write_activity_history(p["activity"], net.activity_history, trial)
+    write_per_neuron_ints(p["replacement"], net.trials_after_replacement, trial)
+    write_per_neuron_ints(p["remodeled"], net.remodeled, trial)
+    write_training(p["training"], p["training_spread"], net.training, net.training_spread)
+    write_num_neurons(p["num_neurons"], n_ra, n_i)
+    write_growth_cfg(p["growth_cfg"], net.syn, net.mat, net.noise, net.conn)
+    c = net.conn
+    write_topology_cfg(p["topology_cfg"], arrangement, c["A_RA2I"], c["SIGMA_RA2I"], c["B_I2RA"], c["SIGMA_I2RA"])

@@ -6,7 +6,7 @@ in the layout the reference keeps on its master rank
 lists (CSR here, in the reference's per-source order), the dense RA->RA weight
 and axonal-delay matrices, the ordered active and super synapse lists, and the
 per-neuron maturation state.  The same object feeds the CUDA library (through
-``unsupervised_growth_gb300.simulator``) and the test oracle.
+``unsupervised_growth_gb300.engine``) and the test oracle.
 
 ``synthetic_*`` build the workloads the benchmark and the parity tests use.
 There is no public dataset for this simulator, so every input is generated
