@@ -29,6 +29,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+METRIC = "trials/s & neuron-RK4-steps/s vs plain FP64 GPU at \u22641-step spike err; p99 lat"
 N_RA, N_I, GROUPS, GROUP, WEIGHT = 2000, 550, 20, 100, 500.0
 NUM_STEPS = 25000
 BATCH = 1024
@@ -44,7 +45,9 @@ MUFU_RA, MUFU_I = 40, 60
 # at 128 trials (16.4 MB read, ~0 written), scaled to a launch of BATCH trials: the state
 # read grows with the trials.
 DRAM_BYTES_RA_PER_TRIAL = 16.4e6 / 128
-CPU_SAMPLE_STEPS = 6000   # first 120 ms of a trial (includes the training kick at 100 ms)
+CPU_WINDOWS = 8   # the headline's CPU baseline advances every core's trial in 8 equal windows
+FP64_BATCH = 64   # test trials per batch of the batched double-precision figure
+SERVE_REQUESTS, SERVE_RATE, SERVE_MAX_TRIALS = 16, 4.0, 10   # the latency leg of the headline
 
 
 def make_network(num_steps=NUM_STEPS):
@@ -62,28 +65,79 @@ def workload_config():
 
 
 # ---------------------------------------------------------------- CPU baseline
-def _cpu_worker(args):
-    trial, steps = args
+def _cpu_proc(conn, first_trial):
+    """One CPU process: the oracle holding the config-3 network, advancing its own
+    test trials window by window on command (None ends it)."""
     sys.path.insert(0, ROOT)
     from oracle.oracle import OracleNet
-    net = make_network(num_steps=steps)
-    onet = OracleNet(net)
-    t0 = time.perf_counter()
-    onet.run_trial(False, trial)
-    return time.perf_counter() - t0
+    onet = OracleNet(make_network())
+    trial = first_trial
+    onet.trial_begin(False, trial)
+    conn.send("ready")
+    while True:
+        n = conn.recv()
+        if n is None:
+            break
+        t0 = time.perf_counter()
+        done = 0
+        while done < n:
+            k = onet.trial_advance(n - done)
+            if k == 0:   # the trial ended inside this window: the next one starts
+                onet.trial_end()
+                trial += 1
+                onet.trial_begin(False, trial)
+                continue
+            done += k
+        conn.send(time.perf_counter() - t0)
+    onet.trial_end()
 
 
-def cpu_sample(cores: int, steps: int = CPU_SAMPLE_STEPS):
-    """Aggregate trials/s of the oracle on `cores` processes, each integrating a
-    `steps`-step prefix of its own trial."""
-    from oracle import oracle as O
-    O.build()
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        times = pool.map(_cpu_worker, [(k, steps) for k in range(cores)])
-    frac = (steps - 1) / (NUM_STEPS - 1)
-    rate = sum(frac / t for t in times)
-    return rate, times
+class CpuArm:
+    """`cores` processes (spawned, so none inherits a CUDA context), each running its
+    own test trials of the config-3 network in the oracle.  A step advances every
+    process by the same number of integration steps; over ceil(24999 / window) steps
+    each process completes a whole trial, so the rate needs no extrapolation."""
+
+    def __init__(self, cores: int, first_trial: int):
+        from oracle import oracle as O
+        O.build()
+        ctx = mp.get_context("spawn")
+        self.conns, self.procs = [], []
+        for c in range(cores):
+            a, b = ctx.Pipe()
+            p = ctx.Process(target=_cpu_proc, args=(b, first_trial + 1000 * c), daemon=True)
+            p.start()
+            self.conns.append(a)
+            self.procs.append(p)
+        for a in self.conns:
+            assert a.recv() == "ready"
+        self.cores = cores
+
+    def step(self, n_steps: int) -> float:
+        """Wall seconds for every process to advance n_steps integration steps."""
+        t0 = time.perf_counter()
+        for a in self.conns:
+            a.send(n_steps)
+        for a in self.conns:
+            a.recv()
+        return time.perf_counter() - t0
+
+    def close(self):
+        for a in self.conns:
+            a.send(None)
+        for p in self.procs:
+            p.join(timeout=60)
+
+
+def cpu_sample(cores: int, windows: int = 8, first_trial: int = 5_000_000):
+    """Trials/s of the oracle on `cores` processes, each integrating one whole 24999-step
+    trial of the config-3 network in `windows` equal windows."""
+    arm = CpuArm(cores, first_trial)
+    w = -(-(NUM_STEPS - 1) // windows)
+    times = [arm.step(w) for _ in range(windows)]
+    arm.close()
+    steps = w * windows
+    return cores * steps / (NUM_STEPS - 1) / sum(times), times
 
 
 # ---------------------------------------------------------------- clocks
@@ -156,6 +210,90 @@ def _fp64_plain(net, device, trial, rn32):
     rn64.free()
     eng64.close()
     return fp64_s, acc
+
+
+def _fp64_batched(net, device, first, batch=FP64_BATCH):
+    """Seconds for one batch of `batch` test trials of the double build with graph replay
+    (after one untimed batch)."""
+    from unsupervised_growth_gb300.engine import Engine
+    eng64 = Engine(precision=64, device=device, use_graphs=True)
+    rn64 = eng64.load_network(net)
+    rn64.run_test_trials(first, batch)
+    eng64.synchronize()
+    t0 = time.perf_counter()
+    rn64.run_test_trials(first + batch, batch)
+    eng64.synchronize()
+    secs = time.perf_counter() - t0
+    rn64.free()
+    eng64.close()
+    return batch, secs
+
+
+def serve_stream(eng, reqs, nets, clk_index=None):
+    """Submit reqs at their arrival times to a started server, adopt and free each
+    network when its request ends; returns the poll records in request order."""
+    ids = [None] * len(reqs)
+    t_start = time.perf_counter()
+
+    def submitter():
+        for k, (r, net) in enumerate(zip(reqs, nets)):
+            delay = t_start + r.arrival - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids[k] = eng.submit(net, r.kind, 0, r.n_trials, True)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    infos = [None] * len(reqs)
+    pending = set(range(len(reqs)))
+    while pending:
+        for k in list(pending):
+            if ids[k] is None:
+                continue
+            info = eng.poll(ids[k])
+            if info["state"] in ("done", "failed"):
+                infos[k] = info
+                pending.discard(k)
+                if info["net_id"] >= 0:
+                    eng.adopt(nets[k], info["net_id"], reqs[k].kind, reqs[k].n_trials).free()
+        time.sleep(0.002)
+    th.join()
+    return infos
+
+
+def _warm_server(eng, request_cls):
+    """One small request of each kind (captures both group graphs)."""
+    for kind in ("growth", "test"):
+        w = request_cls(0.0, kind, 300, 2, 7)
+        info = eng.poll(eng.submit(w.network(), kind, 0, 2, True), 300.0)
+        eng.adopt(w.network(), info["net_id"], kind, 2).free()
+
+
+def serve_leg(device):
+    """The latency part of the metric: a short Poisson stream of growth and test-trial
+    requests through the serving loop (a fresh engine, so the headline engine's state
+    is untouched).  Returns p50/p99 request latency."""
+    import numpy as np
+
+    from unsupervised_growth_gb300.engine import Engine
+    from unsupervised_growth_gb300.workloads import Request, request_stream
+    reqs = request_stream(n_requests=SERVE_REQUESTS, rate_hz=SERVE_RATE, max_trials=SERVE_MAX_TRIALS)
+    nets = [r.network() for r in reqs]
+    eng = Engine(precision=32, device=device)
+    eng.server_start(max_members=64)
+    _warm_server(eng, Request)
+    infos = serve_stream(eng, reqs, nets)
+    eng.server_stop()
+    eng.close()
+    lat = np.array([i["t_done"] - i["t_submit"] for i in infos])
+    t0 = min(i["t_submit"] for i in infos)
+    t1 = max(i["t_done"] for i in infos)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "served_trials_per_s": sum(r.n_trials for r in reqs) / (t1 - t0),
+            "failed": sum(1 for i in infos if i["state"] != "done"),
+            "workload": f"{SERVE_REQUESTS} requests, Poisson arrivals at {SERVE_RATE}/s, HVC-RA log-uniform "
+                        f"200-8000, HVC-I = RA/4, 1-{SERVE_MAX_TRIALS} trials each, growth or test with p = 0.5, "
+                        f"continuous batching in the serving loop (bench.py --workload serve runs the full stream)"}
 
 
 TRIALS_PER_RANK = 1_000_000   # rank r draws the noise streams of trials [r * 1e6, (r + 1) * 1e6)
@@ -268,12 +406,15 @@ def run_ours(args, rank, world, local_rank):
         per_launch = kernels[dom]["fp32_ops_per_launch"]
         achieved = per_launch / (kernels[dom]["avg_launch_ms"] * 1e-3)
 
-        # plain double-precision GPU path: one trial per run, no batching, no graph
+        # plain double-precision GPU path: one trial per run, no batching, no graph;
+        # and the double build batched, to split the speed-up into batching and precision
         fp64 = None if args.skip_fp64 else _fp64_plain(net, local_rank, first, rn)
-        cores = min(os.cpu_count() or 1, 16)
-        cpu_rate, cpu_times = cpu_sample(cores) if not args.skip_cpu else (None, [])
+        fp64_batched = None if args.skip_fp64 else _fp64_batched(net, local_rank, first + 500_000)
+        latency = None if args.skip_serve else serve_leg(local_rank)
+        cores = os.cpu_count() or 1
+        cpu_rate, cpu_times = cpu_sample(cores, CPU_WINDOWS) if not args.skip_cpu else (None, [])
         result = {
-            "metric": "trials/s (500 ms test trials, 2000 RA + 550 I network)",
+            "metric": METRIC,
             "value": value, "unit": "trials/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded network and Philox noise)",
@@ -298,11 +439,23 @@ def run_ours(args, rank, world, local_rank):
             result["fp64_plain_gpu"] = {"trials_per_s": 1.0 / fp64_s, "speedup_of_value": value * fp64_s,
                                         "how": "one trial per run, no batching, no graph, double precision"}
             result["accuracy_vs_fp64"] = acc
+        if fp64_batched is not None:
+            b64, s64 = fp64_batched
+            result["fp64_batched_gpu"] = {"trials_per_s": b64 / s64, "trials_per_batch": b64,
+                                          "speedup_of_value": value / (b64 / s64),
+                                          "how": "the double build with the production batching and graph replay: "
+                                                 "value / this = the single-precision gain, this / fp64_plain_gpu "
+                                                 "= the batching gain"}
+        if latency is not None:
+            result["latency"] = latency
         if cpu_rate is not None:
             result["cpu_baseline"] = {"value": cpu_rate, "unit": "trials/s", "cores": cores, "kind": "port",
-                                      "sample": f"oracle/ (double-precision CPU restatement) on {cores} processes, "
-                                                f"each the first {CPU_SAMPLE_STEPS - 1} steps (120 ms) of its own "
-                                                f"trial of this network; rate scaled by the 24999-step trial"}
+                                      "sample": f"oracle/ (the double-precision CPU port, bit-identical to the "
+                                                f"reference's NetworkGrowthSimulator on the pinned cases) on all "
+                                                f"{cores} host cores, one process per core, each integrating one "
+                                                f"whole 24999-step trial of this network in {CPU_WINDOWS} windows; "
+                                                f"no extrapolation",
+                                      "wall_s": sum(cpu_times)}
     rn.free()
     eng.close()
     if dist:
@@ -563,44 +716,15 @@ def run_serve(args, local_rank):
 
     from unsupervised_growth_gb300 import build as B
     from unsupervised_growth_gb300.engine import Engine
-    from unsupervised_growth_gb300.workloads import request_stream
+    from unsupervised_growth_gb300.workloads import Request, request_stream
     B.build()
     reqs = request_stream(n_requests=args.requests, rate_hz=args.rate)
     nets = [r.network() for r in reqs]
     eng = Engine(precision=32, device=local_rank)
     eng.server_start(max_members=args.members)
-    # warm-up: one small request of each kind (graph capture of both group graphs)
-    for kind in ("growth", "test"):
-        w = reqs[0].__class__(0.0, kind, 300, 2, 7)
-        info = eng.poll(eng.submit(w.network(), kind, 0, 2, True), 300.0)
-        eng.adopt(w.network(), info["net_id"], kind, 2).free()
-    ids = [None] * len(reqs)
-    t_start = time.perf_counter()
-
-    def submitter():
-        for k, (r, net) in enumerate(zip(reqs, nets)):
-            delay = t_start + r.arrival - time.perf_counter()
-            if delay > 0:
-                time.sleep(delay)
-            ids[k] = eng.submit(net, r.kind, 0, r.n_trials, True)
-
-    th = threading.Thread(target=submitter)
+    _warm_server(eng, Request)
     with ClockSampler(local_rank) as clk:
-        th.start()
-        infos = [None] * len(reqs)
-        pending = set(range(len(reqs)))
-        while pending:
-            for k in list(pending):
-                if ids[k] is None:
-                    continue
-                info = eng.poll(ids[k])
-                if info["state"] in ("done", "failed"):
-                    infos[k] = info
-                    pending.discard(k)
-                    if info["net_id"] >= 0:
-                        eng.adopt(nets[k], info["net_id"], reqs[k].kind, reqs[k].n_trials).free()
-            time.sleep(0.002)
-        th.join()
+        infos = serve_stream(eng, reqs, nets)
     eng.server_stop()
     failed = [i for i in infos if i["state"] != "done"]
     lat = np.array([i["t_done"] - i["t_submit"] for i in infos])
@@ -702,24 +826,36 @@ def run_topology(args, local_rank):
 
 
 def run_reference(args, rank):
+    """The CPU path of the reference on the host cores, for the config-3 workload: every
+    core runs its own test trials of the 2000 / 550 chain network in the double-precision
+    CPU port (oracle/), which tests/test_reference_sim.py shows bit-identical to the
+    reference's own NetworkGrowthSimulator.  The reference's trial code itself needs the
+    reference tree, which is not on the GPU host.  A step advances every core by
+    ceil(24999 / steps) integration steps, so the timed steps cover one whole trial per
+    core; the warm-up steps advance a separate warm-up trial by 200 steps each."""
     if rank != 0:
         return None
-    cores = min(os.cpu_count() or 1, 16)
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
-    rates = []
-    for _ in range(args.steps):
-        r, _ = cpu_sample(cores)
-        rates.append(r)
-    value = statistics.mean(rates)
-    return {"impl": "reference", "metric": "trials/s (500 ms test trials, 2000 RA + 550 I network)", "value": value,
+    cores = os.cpu_count() or 1
+    window = -(-(NUM_STEPS - 1) // max(args.steps, 1))
+    warm = CpuArm(cores, 6_000_000)
+    for _ in range(args.warmup):
+        warm.step(200)
+    warm.close()
+    arm = CpuArm(cores, 7_000_000)
+    times = [arm.step(window) for _ in range(args.steps)]
+    arm.close()
+    trials = cores * window * args.steps / (NUM_STEPS - 1)
+    value = trials / sum(times)
+    sample = (f"all {cores} host cores, one process per core, each advancing its own 24999-step test trial of the "
+              f"config-3 network by {window} steps per step; {args.steps} steps = {trials / cores:.3f} trial per core; "
+              f"oracle/ (the double-precision CPU port, bit-identical to the reference's NetworkGrowthSimulator on "
+              f"the pinned cases)")
+    return {"impl": "reference", "metric": METRIC, "value": value,
             "unit": "trials/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 / value if value else None, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded network and Philox noise)",
-            "config": dict(workload_config(), parallelism=f"cpu{cores}"),
-            "cpu_baseline": {"value": value, "unit": "trials/s", "cores": cores, "kind": "port",
-                             "sample": f"each step: {cores} processes, each the first {CPU_SAMPLE_STEPS - 1} steps "
-                                       f"of its own trial, scaled by the 24999-step trial"},
+            "config": dict(workload_config(), parallelism=f"cpu{cores}", trials_per_step=trials / args.steps),
+            "cpu_baseline": {"value": value, "unit": "trials/s", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "trials/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -750,9 +886,19 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
     ap.add_argument("--skip-fp64", action="store_true", help="do not time the plain double-precision GPU path")
+    ap.add_argument("--skip-serve", action="store_true", help="do not run the serving-latency leg of the headline")
     args = ap.parse_args()
+    if args.gpus > 1 and "RANK" not in os.environ:
+        # one process per GPU: relaunch under torch.distributed.run on this node
+        import socket
+        with socket.socket() as sk:
+            sk.bind(("127.0.0.1", 0))
+            port = sk.getsockname()[1]
+        cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+               "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+        raise SystemExit(subprocess.call(cmd))
     rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", args.gpus if "RANK" in os.environ else 1))
+    world = int(os.environ.get("WORLD_SIZE", 1))
     local_rank = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         res = run_reference(args, rank)

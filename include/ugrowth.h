@@ -303,6 +303,8 @@ ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms
  * device array that every GPU loading this library holds until exit; networks needing more
  * (a network of 1000 HVC(RA) and 250 HVC(I) neurons with delays up to 10 ms fits) get UG_EINVAL.  Outputs are caller-owned device
  * arrays: soma/dend count and first step [n_ra], interneuron count and first step [n_i].
+ * Its spike record holds 16 spikes per neuron whatever capacity the network was loaded
+ * with; a trial that needs more returns UG_ECAPACITY.
  * The first call on a device resolves the array's address (make it before any stream
  * capture).  Every call shares the array: calls that overlap on the GPU race.  Returns
  * after the trial has finished; UG_EINVAL for a double-precision context or when growth

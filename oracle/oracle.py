@@ -122,6 +122,11 @@ def lib():
         L.ugo_get_delivery_log.argtypes = [C.c_void_p, _i32p, C.c_int64]
         L.ugo_run_trial.restype = C.c_int32
         L.ugo_run_trial.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]
+        for f in (L.ugo_trial_begin, L.ugo_trial_advance, L.ugo_trial_end):
+            f.restype = C.c_int32
+        L.ugo_trial_begin.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]
+        L.ugo_trial_advance.argtypes = [C.c_void_p, C.c_int32]
+        L.ugo_trial_end.argtypes = [C.c_void_p]
         L.ugo_after_growth_trial.restype = C.c_int32
         L.ugo_after_growth_trial.argtypes = [C.c_void_p, C.c_uint32]
         L.ugo_get_spikes.restype = C.c_int64
@@ -374,6 +379,17 @@ class OracleNet:
 
     def run_trial(self, growth: bool, trial_index: int, training: bool = True) -> int:
         return self.L.ugo_run_trial(self.h, 1 if growth else 0, 1 if training else 0, trial_index)
+
+    def trial_begin(self, growth: bool, trial_index: int, training: bool = True) -> int:
+        """Start a trial on a worker thread, paused before its first integration step."""
+        return self.L.ugo_trial_begin(self.h, 1 if growth else 0, 1 if training else 0, trial_index)
+
+    def trial_advance(self, n_steps: int) -> int:
+        """Run n_steps more steps of the started trial; returns the steps run (0 once it ended)."""
+        return self.L.ugo_trial_advance(self.h, n_steps)
+
+    def trial_end(self) -> int:
+        return self.L.ugo_trial_end(self.h)
 
     def after_growth_trial(self, trial_index: int) -> int:
         return self.L.ugo_after_growth_trial(self.h, trial_index)

@@ -11,8 +11,12 @@
 #include "ug_oracle.h"
 #include "ugo_noise.h"
 
+#include <climits>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 #include <algorithm>
 #include <utility>
@@ -487,6 +491,17 @@ struct ugo_net {
     std::vector<int> delivery_log;
 
     std::vector<ugo_stream> ra_noise, i_noise;
+
+    /* Step gate of a trial run on a worker thread (ugo_trial_begin / _advance / _end):
+     * the trial waits before step t until t < gate_until. */
+    std::mutex gate_mu;
+    std::condition_variable gate_cv;
+    bool gated = false;
+    int gate_until = INT_MAX;
+    int gate_at = 0;          /* the step the trial waits at; num_steps once it has finished */
+    bool gate_done = false;
+    int gate_rc = 0;
+    std::thread gate_worker;
 };
 
 namespace {
@@ -658,6 +673,12 @@ int run_trial(ugo_net* net, bool growth, bool training, uint32_t trial)
     }
 
     for (int t = 1; t < num_steps; ++t) {
+        if (net->gated) {
+            std::unique_lock<std::mutex> lk(net->gate_mu);
+            net->gate_at = t;
+            net->gate_cv.notify_all();
+            net->gate_cv.wait(lk, [&] { return t < net->gate_until; });
+        }
         internal_time += TIMESTEP;
         for (int i = 0; i < NRA; ++i) {
             RAState& s = net->ra[i];
@@ -1128,7 +1149,11 @@ ugo_net* ugo_new(int32_t n_ra, int32_t n_i)
     return net;
 }
 
-void ugo_free(ugo_net* net) { delete net; }
+void ugo_free(ugo_net* net)
+{
+    if (net->gate_worker.joinable()) ugo_trial_end(net);
+    delete net;
+}
 
 void ugo_set_params(ugo_net* net, const ugo_synaptic_params* syn, const ugo_maturation_params* mat,
                     const ugo_noise_params* noise, const ugo_connection_params* conn)
@@ -1250,6 +1275,52 @@ int64_t ugo_get_delivery_log(const ugo_net* net, int32_t* out3, int64_t cap)
 int32_t ugo_run_trial(ugo_net* net, int32_t kind, int32_t training, uint32_t trial_index)
 {
     return run_trial(net, kind == 1, training != 0, trial_index);
+}
+
+int32_t ugo_trial_begin(ugo_net* net, int32_t kind, int32_t training, uint32_t trial_index)
+{
+    if (net->gate_worker.joinable()) return -2;
+    {
+        std::lock_guard<std::mutex> lk(net->gate_mu);
+        net->gated = true;
+        net->gate_until = 1;
+        net->gate_at = 0;
+        net->gate_done = false;
+    }
+    net->gate_worker = std::thread([=] {
+        int rc = run_trial(net, kind == 1, training != 0, trial_index);
+        std::lock_guard<std::mutex> lk(net->gate_mu);
+        net->gate_rc = rc;
+        net->gate_at = net->num_steps;
+        net->gate_done = true;
+        net->gate_cv.notify_all();
+    });
+    std::unique_lock<std::mutex> lk(net->gate_mu);
+    net->gate_cv.wait(lk, [&] { return net->gate_at >= 1 || net->gate_done; });
+    return 0;
+}
+
+int32_t ugo_trial_advance(ugo_net* net, int32_t n_steps)
+{
+    std::unique_lock<std::mutex> lk(net->gate_mu);
+    if (!net->gated || net->gate_done) return 0;
+    const int from = net->gate_at;
+    net->gate_until = from + n_steps;
+    net->gate_cv.notify_all();
+    net->gate_cv.wait(lk, [&] { return net->gate_at >= net->gate_until || net->gate_done; });
+    return (net->gate_done ? net->num_steps : net->gate_at) - from;
+}
+
+int32_t ugo_trial_end(ugo_net* net)
+{
+    {
+        std::lock_guard<std::mutex> lk(net->gate_mu);
+        net->gate_until = INT_MAX;
+        net->gate_cv.notify_all();
+    }
+    if (net->gate_worker.joinable()) net->gate_worker.join();
+    net->gated = false;
+    return net->gate_rc;
 }
 
 int32_t ugo_after_growth_trial(ugo_net* net, uint32_t trial_index)

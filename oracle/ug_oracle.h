@@ -106,6 +106,14 @@ int64_t ugo_get_delivery_log(const ugo_net* net, int32_t* out3, int64_t capacity
  * trial_index selects the noise streams.  Returns 0, or -1 when
  * check_bad_values fails afterwards. */
 int32_t ugo_run_trial(ugo_net* net, int32_t kind, int32_t training, uint32_t trial_index);
+/* The same trial on a worker thread, advanced in windows of integration steps (the CPU
+ * baseline of the benchmark times equal slices of whole trials this way).  begin starts the
+ * trial and returns once its set-up is done and it waits before step 1; advance lets it run
+ * n_steps more steps and returns the number run (fewer at the trial's end, 0 once it has
+ * ended); end waits for the trial to finish and returns run_trial's result. */
+int32_t ugo_trial_begin(ugo_net* net, int32_t kind, int32_t training, uint32_t trial_index);
+int32_t ugo_trial_advance(ugo_net* net, int32_t n_steps);
+int32_t ugo_trial_end(ugo_net* net);
 /* The per-trial tail of chain_growth (NetworkGrowthSimulator.cpp:5841-5875):
  * trial counters, check_neuron_activity, maturation, replacement, reset.
  * Returns the number of replaced neurons. */

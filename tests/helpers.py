@@ -34,3 +34,14 @@ def growth_net(seed=7, replace_ids=(), syn=None):
 def oracle_trial_spikes(onet, which):
     n, s = onet.spikes(which)
     return sorted_spikes(n, s)
+
+
+def heavy_growth_net(seed, width, delays="uniform", n_tr=20):
+    """A 1100 / 275 fast-growth network: at least 1024 HVC(RA), so in a group its spiking
+    rows take the block-per-row delivery path.  Twenty training neurons spread over
+    15 ms, so training rows potentiate onto one another within a trial."""
+    net = small_growth(seed=seed, n_ra=1100, n_i=275, n_tr=n_tr, syn=FAST_SYN, mat=FAST_MAT, delays=delays,
+                       delay_width=width)
+    net.training_spread = np.linspace(0.0, 15.0, len(net.training))
+    net.trials_after_replacement[net.training] = 0
+    return net

@@ -145,3 +145,33 @@ def test_shipped_flags_build_agrees():
     a, b = RefSimNet(net, opt="O0"), RefSimNet(net, opt="O2")
     assert a.run_trial(False, 2) == 0 and b.run_trial(False, 2) == 0
     assert same_spikes(a, b)
+
+
+def test_golden_reference_runs_rebuild_the_same_networks():
+    """tests/golden/reference_runs.npz was made by the reference simulator on networks
+    rebuilt from seeds; the same seeds must give the same networks here."""
+    import os
+
+    from tests.helpers import heavy_growth_net
+    from unsupervised_growth_gb300.workloads import config1_network, config3_network, network_fingerprint
+    data = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_runs.npz"))
+    for name, make in (("config3", config3_network), ("config1", config1_network),
+                       ("heavy0", lambda: heavy_growth_net(41, 0.0)), ("heavy1", lambda: heavy_growth_net(42, 0.5))):
+        assert str(data[f"{name}__fingerprint"]) == network_fingerprint(make()), name
+
+
+def test_oracle_reproduces_golden_config1_trial():
+    """The oracle gives the stored reference result of the first config-1 growth trial."""
+    import os
+
+    from unsupervised_growth_gb300.workloads import config1_network
+    data = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_runs.npz"))
+    net = config1_network()
+    o = OracleNet(net)
+    assert o.run_trial(True, 0) == 0
+    o.after_growth_trial(0)
+    for w in (0, 1, 2):
+        assert np.array_equal(oracle_trial_spikes(o, w), data[f"config1__t0__spk{w}"]), w
+    W = o.weights().ravel()
+    idx = np.flatnonzero(W)
+    assert np.array_equal(idx, data["config1__t0__w_idx"]) and np.array_equal(W[idx], data["config1__t0__w_val"])

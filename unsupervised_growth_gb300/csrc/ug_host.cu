@@ -537,6 +537,12 @@ template <class R>
 ug_status NetImpl<R>::ensure_batch(int B)
 {
     if (B <= B_cap_) return UG_OK;
+    // Growing frees each old buffer before allocating its successor, so a failure
+    // part-way must leave no capacity, graph or device pointer behind that names
+    // freed memory: a later call then allocates again instead of running on them.
+    B_cap_ = 0;
+    drop_graphs();
+    bd_ = ug::BatchDev<R>();
     const size_t nra = (size_t)B * h.n_ra, ni = (size_t)B * h.n_i;
     for (int k = 0; k < 10; ++k) UG_TRY(ra_[k].alloc(nra * sizeof(R)));
     for (DevMem* m : {&ra_flags_, &kick_step_, &ra_nsoma_, &ra_ndend_, &ra_first_soma_, &ra_first_dend_}) UG_TRY(m->alloc(nra * sizeof(int)));
@@ -978,6 +984,10 @@ ug_status NetImpl<R>::set_inhibition_tracking(double resolution, cudaStream_t st
             if (pos < points) slot[st_] = pos;
             ++pos;
         }
+    // Tracking stays off until the slot table and the record both exist: a failed
+    // allocation below must not leave a slot table beside a freed record.
+    ginh_res_ = 0.0;
+    ginh_points_ = 0;
     UG_TRY(gGinhSlot_.upload(slot, st));
     UG_TRY(gGinh_.alloc((size_t)points * h.n_ra * sizeof(R)));
     UG_CUDA(cudaMemsetAsync(gGinh_.as<R>(), 0, (size_t)points * h.n_ra * sizeof(R), st));

@@ -369,7 +369,7 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
             soma |= (uint32_t)fs << (st - s0);
             dend |= (uint32_t)fd << (st - s0);
             if constexpr (kTrack) {   // inhibition tracking; a group may mix tracked and untracked members
-                if (bt.ginh_slot) {
+                if (bt.ginh_slot && bt.ginh_rec) {
                     const int sl = bt.ginh_slot[st];
                     if (sl > 0) bt.ginh_rec[(size_t)sl * bt.B * n.n_ra + x] = s.Gi;
                 }
@@ -478,7 +478,7 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
                             make_float2(ra_point_f(w0.y), ra_point_f(w1.y)), make_float2(ra_point_f(w0.z), ra_point_f(w1.z)),
                             make_float2(ra_point_f(w0.w), ra_point_f(w1.w)));
             if constexpr (kTrack) {   // inhibition tracking; a group may mix tracked and untracked members
-                if (bt.ginh_slot) {
+                if (bt.ginh_slot && bt.ginh_rec) {
                     const int sl = bt.ginh_slot[st];
                     if (sl > 0) {
                         R* rec = bt.ginh_rec + (size_t)sl * bt.B * n.n_ra;

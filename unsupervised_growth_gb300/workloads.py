@@ -72,3 +72,52 @@ def request_stream(n_requests=48, rate_hz=2.0, seed=5, lo=200, hi=8000, max_tria
     kinds = np.where(rng.random(n_requests) < growth_fraction, "growth", "test")
     return [Request(float(a), str(k), int(s), int(t), seed * 10000 + i)
             for i, (a, k, s, t) in enumerate(zip(arrivals, kinds, sizes, trials))]
+
+
+# ------------------------------------------------------------ named configurations
+# Config 1: a plain growth trial of 300 HVC(RA) / 100 HVC(I) on a sphere, uniform
+# 0-2 ms delays, white noise sigma 0.1 / 0.2, ten mature training neurons, the STDP
+# set of the network defaults (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold
+# 0.035, Nss 3).
+def config1_network(seed: int = 1) -> Network:
+    return synthetic_growth_network(n_ra=300, n_i=100, n_tr=10, seed=seed, delays="uniform", delay_width=2.0)
+
+
+# Config 2: growth at scale, 2000 / 550 with log-normal delays (mean 3, sd 1.5, cap 10 ms).
+def config2_network(seed: int = 2, syn=None, mat=None) -> Network:
+    extra = {}
+    if syn:
+        extra["syn"] = syn
+    if mat:
+        extra["mat"] = mat
+    return synthetic_growth_network(n_ra=2000, n_i=550, n_tr=10, seed=seed, delays="lognormal", lognormal_mean=3.0,
+                                    lognormal_sigma=1.5, delay_cap=10.0, **extra)
+
+
+# Config 3: the fixed grown 2000 / 550 network for batched test trials: a synfire chain
+# of 20 groups x 100 neurons, 0.05 mS/cm^2 per synapse between consecutive groups
+# (500 in the reference's weight units, which raiseExcWeight divides by the
+# 10000 um^2 dendritic area), log-normal delays mean 3 ms.
+CONFIG3 = dict(n_ra=2000, n_i=550, n_groups=20, group_size=100, weight=500.0, seed=3)
+
+
+def config3_network(num_steps: int = 25000) -> Network:
+    return synthetic_chain_network(delays="lognormal", lognormal_mean=3.0, lognormal_sigma=1.5, delay_cap=10.0,
+                                   num_steps=num_steps, **CONFIG3)
+
+
+def network_fingerprint(net: Network) -> str:
+    """SHA-256 over every array and parameter of a network, so a result stored for a
+    seeded network can be matched to the network rebuilt on another machine."""
+    import hashlib
+    h = hashlib.sha256()
+    for k in sorted(vars(net)):
+        v = getattr(net, k)
+        if isinstance(v, np.ndarray):
+            h.update(k.encode())
+            h.update(np.ascontiguousarray(v).tobytes())
+        elif isinstance(v, dict):
+            h.update(repr(sorted(v.items())).encode())
+        else:
+            h.update(repr((k, v)).encode())
+    return h.hexdigest()
