@@ -303,11 +303,11 @@ def i_single(n_steps, seed=1, trial=0, neuron=0, kicks=None, use_ref=False):
 class OracleNet:
     """One network held by the CPU restatement; mirrors the simulator's state."""
 
-    def __init__(self, net, L=None):
+    def __init__(self, net, L=None, handle=None):
         """net: a unsupervised_growth_gb300.network.Network-like object (numpy arrays)."""
         self.L = L if L is not None else lib()
         self.n_ra, self.n_i = net.n_ra, net.n_i
-        self.h = self.L.ugo_new(self.n_ra, self.n_i)
+        self.h = handle if handle is not None else self.L.ugo_new(self.n_ra, self.n_i)
         self.window = int(net.mat["RATE_WINDOW_LONG"])
         syn = SynapticParams(**net.syn)
         mat = MaturationParams(**net.mat)
@@ -488,3 +488,74 @@ class RefSimNet(OracleNet):
         self.n_ra, self.n_i = n_ra.value, n_i.value
         R.refsim_set_seed(self.h, int(seed), int(net_id))
         return self
+
+
+class RefSimWorldNet(OracleNet):
+    """The reference's neuron-partitioned mode (`mpirun -np ranks`) with ranks as threads of
+    the thread-backed MPI stand-in: set-up on rank 0, trials and getters over every rank."""
+
+    def __init__(self, net, ranks: int, opt: str = "O2"):
+        R = ref_sim_lib(opt)
+        if R is None:
+            raise RuntimeError("the reference simulator is not built (oracle/Makefile target refsim)")
+        R.refsim_world_new.restype = C.c_void_p
+        R.refsim_world_new.argtypes = [C.c_int32, C.c_int32, C.c_int32]
+        R.refsim_world_free.argtypes = [C.c_void_p]
+        R.refsim_world_master.restype = C.c_void_p
+        R.refsim_world_master.argtypes = [C.c_void_p]
+        R.refsim_world_set_seed.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32]
+        for f in (R.refsim_world_run_trial, R.refsim_world_after_growth_trial):
+            f.restype = C.c_int32
+        R.refsim_world_run_trial.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint32]
+        R.refsim_world_after_growth_trial.argtypes = [C.c_void_p, C.c_uint32]
+        R.refsim_world_get_spikes.restype = C.c_int64
+        R.refsim_world_get_spikes.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, C.c_int64]
+        R.refsim_world_get_weights.argtypes = [C.c_void_p, _f64p]
+        R.refsim_world_get_list.restype = C.c_int64
+        R.refsim_world_get_list.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p]
+        R.refsim_world_get_neuron_props.argtypes = [C.c_void_p, _f64p, _f64p, _i32p, _f64p, _i32p, _i32p, _f64p]
+        self.R = R
+        self.w = R.refsim_world_new(int(ranks), int(net.n_ra), int(net.n_i))
+        super().__init__(net, L=_Prefixed(R), handle=R.refsim_world_master(self.w))
+        R.refsim_world_set_seed(self.w, int(net.seed), int(net.net_id))
+
+    def __del__(self):
+        if getattr(self, "w", None):
+            self.R.refsim_world_free(self.w)
+            self.w = None
+            self.h = None
+
+    def run_trial(self, growth: bool, trial_index: int, training: bool = True) -> int:
+        return self.R.refsim_world_run_trial(self.w, 1 if growth else 0, 1 if training else 0, trial_index)
+
+    def after_growth_trial(self, trial_index: int) -> int:
+        return self.R.refsim_world_after_growth_trial(self.w, trial_index)
+
+    def spikes(self, which: int):
+        n = self.R.refsim_world_get_spikes(self.w, which, None, None, 0)
+        nn = np.zeros(n, dtype=np.int32)
+        ss = np.zeros(n, dtype=np.int32)
+        self.R.refsim_world_get_spikes(self.w, which, _ptr(nn, _i32p), _ptr(ss, _i32p), n)
+        return nn, ss
+
+    def weights(self):
+        w = np.zeros((self.n_ra, self.n_ra), dtype=np.float64)
+        self.R.refsim_world_get_weights(self.w, _ptr(w, _f64p))
+        return w
+
+    def synapse_list(self, which: int):
+        n = self.R.refsim_world_get_list(self.w, which, None, None)
+        off = np.zeros(self.n_ra + 1, dtype=np.int32)
+        tgt = np.zeros(max(n, 1), dtype=np.int32)
+        self.R.refsim_world_get_list(self.w, which, _ptr(off, _i32p), _ptr(tgt, _i32p))
+        return [tgt[off[i]:off[i + 1]].tolist() for i in range(self.n_ra)]
+
+    def neuron_props(self):
+        N = self.n_ra
+        rest, gca, scale, frl = (np.zeros(N) for _ in range(4))
+        mature, remod, tar = (np.zeros(N, dtype=np.int32) for _ in range(3))
+        self.R.refsim_world_get_neuron_props(self.w, _ptr(rest, _f64p), _ptr(gca, _f64p), _ptr(mature, _i32p),
+                                             _ptr(scale, _f64p), _ptr(remod, _i32p), _ptr(tar, _i32p),
+                                             _ptr(frl, _f64p))
+        return dict(rest_potential=rest, gca=gca, mature=mature, maturation_scale=scale, remodeled=remod,
+                    trials_after_replacement=tar, firing_rate_long=frl)

@@ -43,6 +43,22 @@
 
 namespace {
 
+/* Silences std::cout (the reference reports every trial there) for one scope.  Ranks run
+ * as threads in a world share std::cout, so there the world silences it once instead. */
+struct Quiet {
+    bool on;
+    std::ostringstream sink;
+    std::streambuf* old = nullptr;
+    explicit Quiet(bool enable) : on(enable)
+    {
+        if (on) old = std::cout.rdbuf(sink.rdbuf());
+    }
+    ~Quiet()
+    {
+        if (on) std::cout.rdbuf(old);
+    }
+};
+
 class RefSim : public NetworkGrowthSimulator {
 public:
     RefSim(int n_ra, int n_i)
@@ -57,6 +73,7 @@ public:
     uint64_t seed = 0;
     uint32_t net_id = 0;
     bool initialized = false;
+    bool own_stdout = true;   /* false for the ranks of a world */
     std::vector<Poisson_noise> ra_gen, i_gen;
     std::vector<double> spread;
     std::vector<int> replaced;
@@ -129,10 +146,13 @@ public:
     void ensure_initialized()
     {
         if (initialized) return;
-        std::ostringstream sink;
-        std::streambuf* old = std::cout.rdbuf(sink.rdbuf());
-        initialize_network();
-        std::cout.rdbuf(old);
+        {
+            Quiet q(own_stdout);
+            /* continue_chain_growth broadcasts the parameters read on rank 0 before
+             * initialize_network (:2042-2043); with one rank this is a no-op */
+            send_growth_parameters();
+            initialize_network();
+        }
         spread.assign(N_RA, 0.0);
         for (int i = 0; i < N_TR; ++i) spread[training_neurons[i]] = training_spread_times[i];
         ra_gen.resize(N_RA_local);
@@ -165,8 +185,7 @@ public:
     {
         ensure_initialized();
         bind_streams(trial);
-        std::ostringstream sink;
-        std::streambuf* old = std::cout.rdbuf(sink.rdbuf());
+        Quiet q(own_stdout);
         if (kind == 0) {
             reset_after_chain_test();
             trial_no_stdp_fixedSpread(spread);
@@ -175,14 +194,12 @@ public:
             noise_generator.bind(seed, UGO_KIND_TRIAL, net_id, 0, trial);
             trial_1stSoma_pre_1stSoma_post_delays_fixedSpread(training, spread);
         }
-        std::cout.rdbuf(old);
         return check_bad_values() < 0 ? -1 : 0;
     }
 
     int after_growth_trial(uint32_t trial)
     {
-        std::ostringstream sink;
-        std::streambuf* old = std::cout.rdbuf(sink.rdbuf());
+        Quiet q(own_stdout);
         for (int i = 0; i < N_RA_local; i++) num_trials_after_replacement_local[i] += 1;
         std::vector<int> neurons_to_replace;
         check_neuron_activity(neurons_to_replace);
@@ -191,7 +208,6 @@ public:
             noise_generator.bind(seed, UGO_KIND_REPLACE, net_id, 0, trial);
             replace_neurons(neurons_to_replace);
         }
-        std::cout.rdbuf(old);
         replaced = neurons_to_replace;
         return (int)neurons_to_replace.size();
     }
@@ -354,6 +370,8 @@ public:
         }
     }
 
+    void sizes_local(int* n_ra_local) const { *n_ra_local = N_RA_local; }
+
     void sizes(int32_t* n_ra, int32_t* n_i) const
     {
         *n_ra = N_RA;
@@ -470,6 +488,148 @@ int64_t refsim_get_replaced(void* h, int32_t* out, int64_t cap)
     const std::vector<int>& r = S(h)->replaced;
     for (int64_t k = 0; out && k < (int64_t)r.size() && k < cap; ++k) out[k] = r[k];
     return (int64_t)r.size();
+}
+
+} // extern "C"
+
+/* ---- The reference's neuron-partitioned mode over thread ranks ----------------------------
+ * K instances of the simulator, one per rank thread of the thread-backed MPI stand-in
+ * (ref_shim/mpi_threads.cpp), run the reference's own `mpirun -np K` code path: neurons
+ * split across ranks by initialize_network (:745-890), kicks summed by MPI_Allreduce every
+ * 0.25 ms, parameters, connections and synapse lists scattered from rank 0.  Set-up goes to
+ * rank 0 alone (as read_network_state runs on rank 0 only, :2039-2040); trials, the per-trial
+ * tail and the getters cover every rank. */
+#include <thread>
+#include "mpi.h"
+
+namespace {
+
+struct RefWorld {
+    int K;
+    std::vector<RefSim*> sims;
+
+    template <class F>
+    void ranks(F f)
+    {
+        std::vector<std::thread> th;
+        for (int r = 0; r < K; ++r)
+            th.emplace_back([&, r] {
+                ugmpi_set_rank(r);
+                f(r, sims[(size_t)r]);
+            });
+        for (auto& t : th) t.join();
+        ugmpi_set_rank(0);
+    }
+
+    RefWorld(int k, int n_ra, int n_i) : K(k), sims((size_t)k, nullptr)
+    {
+        ugmpi_init_world(K);
+        std::vector<std::thread> th;
+        for (int r = 0; r < K; ++r)
+            th.emplace_back([&, r] {
+                ugmpi_set_rank(r);   /* the simulator's constructor asks MPI for its rank */
+                sims[(size_t)r] = new RefSim(n_ra, n_i);
+                sims[(size_t)r]->own_stdout = false;
+            });
+        for (auto& t : th) t.join();
+        ugmpi_set_rank(0);
+    }
+
+    ~RefWorld()
+    {
+        for (RefSim* s : sims) delete s;
+        ugmpi_init_world(1);
+    }
+};
+
+RefWorld* Wd(void* h) { return static_cast<RefWorld*>(h); }
+
+} // namespace
+
+extern "C" {
+
+/* A world of `ranks` thread ranks; the set-up calls below take its rank-0 instance
+ * (refsim_world_master) like the single-rank ones. */
+void* refsim_world_new(int32_t ranks, int32_t n_ra, int32_t n_i) { return new RefWorld(ranks, n_ra, n_i); }
+void refsim_world_free(void* w) { delete Wd(w); }
+void* refsim_world_master(void* w) { return Wd(w)->sims[0]; }
+
+void refsim_world_set_seed(void* w, uint64_t seed, uint32_t net_id)
+{
+    for (RefSim* s : Wd(w)->sims) {
+        s->seed = seed;
+        s->net_id = net_id;
+    }
+}
+
+int32_t refsim_world_run_trial(void* w, int32_t kind, int32_t training, uint32_t trial)
+{
+    std::vector<int> rc((size_t)Wd(w)->K, 0);
+    Quiet q(true);
+    Wd(w)->ranks([&](int r, RefSim* s) { rc[(size_t)r] = s->run_trial(kind, training != 0, trial); });
+    for (int v : rc)
+        if (v) return v;
+    return 0;
+}
+
+int32_t refsim_world_after_growth_trial(void* w, uint32_t trial)
+{
+    std::vector<int> n((size_t)Wd(w)->K, 0);
+    Quiet q(true);
+    Wd(w)->ranks([&](int r, RefSim* s) { n[(size_t)r] = s->after_growth_trial(trial); });
+    return n[0];
+}
+
+int64_t refsim_world_get_spikes(void* w, int32_t which, int32_t* neuron, int32_t* step, int64_t cap)
+{
+    std::vector<std::pair<int, int>> all;
+    for (RefSim* s : Wd(w)->sims) {
+        int64_t n = s->spikes(which, nullptr, nullptr, 0);
+        std::vector<int32_t> nn((size_t)n), ss((size_t)n);
+        s->spikes(which, nn.data(), ss.data(), n);
+        for (int64_t k = 0; k < n; ++k) all.emplace_back(ss[(size_t)k], nn[(size_t)k]);
+    }
+    std::sort(all.begin(), all.end());
+    if (neuron && step)
+        for (int64_t k = 0; k < (int64_t)all.size() && k < cap; ++k) {
+            step[k] = all[(size_t)k].first;
+            neuron[k] = all[(size_t)k].second;
+        }
+    return (int64_t)all.size();
+}
+
+void refsim_world_get_weights(void* w, double* out)
+{
+    for (RefSim* s : Wd(w)->sims) s->weights(out);
+}
+
+/* Ranks own consecutive HVC(RA) ids in rank order, so their lists concatenate in id order. */
+int64_t refsim_world_get_list(void* w, int32_t which, int32_t* off, int32_t* tgt)
+{
+    int64_t total = 0;
+    int row = 0;
+    for (RefSim* s : Wd(w)->sims) {
+        int64_t n = s->list(which, nullptr, nullptr);
+        std::vector<int32_t> o, t((size_t)std::max<int64_t>(n, 1));
+        int rows = 0;
+        s->sizes_local(&rows);
+        o.resize((size_t)rows + 1);
+        s->list(which, o.data(), t.data());
+        for (int i = 0; i < rows; ++i) {
+            if (off) off[row + i] = (int32_t)(total + o[(size_t)i]);
+        }
+        if (tgt) std::copy(t.begin(), t.begin() + n, tgt + total);
+        total += n;
+        row += rows;
+    }
+    if (off) off[row] = (int32_t)total;
+    return total;
+}
+
+void refsim_world_get_neuron_props(void* w, double* rest, double* gca, int32_t* mature, double* scale,
+                                   int32_t* remodeled, int32_t* trials_after, double* frl)
+{
+    for (RefSim* s : Wd(w)->sims) s->neuron_props(rest, gca, mature, scale, remodeled, trials_after, frl);
 }
 
 } // extern "C"

@@ -175,3 +175,25 @@ def test_oracle_reproduces_golden_config1_trial():
     W = o.weights().ravel()
     idx = np.flatnonzero(W)
     assert np.array_equal(idx, data["config1__t0__w_idx"]) and np.array_equal(W[idx], data["config1__t0__w_val"])
+
+
+@pytest.mark.parametrize("ranks", [2, 3])
+def test_reference_rank_partitioned_mode(ranks):
+    """The reference's own `mpirun -np K` path (neurons split across ranks, kicks summed by
+    MPI_Allreduce at every synchronisation, set-up scattered from rank 0) with the ranks as
+    threads of the thread-backed MPI stand-in: the same test trial, and the same growth
+    trials with a replacement, as the oracle."""
+    from oracle.oracle import RefSimWorldNet
+    net = small_chain()
+    o, w = OracleNet(net), RefSimWorldNet(net, ranks)
+    assert o.run_trial(False, 1) == 0 and w.run_trial(False, 1) == 0
+    assert same_spikes(o, w)
+    del w
+    probe = growth_net(seed=11)
+    silent = [i for i in range(probe.n_ra) if i not in set(probe.training.tolist())][:3]
+    net = growth_net(seed=11, replace_ids=silent)
+    o, w = OracleNet(net), RefSimWorldNet(net, ranks)
+    for t in range(2):
+        assert o.run_trial(True, t) == 0 and w.run_trial(True, t) == 0
+        assert o.after_growth_trial(t) == w.after_growth_trial(t)
+        assert_same_state(o, w, t)
