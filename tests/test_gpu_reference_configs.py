@@ -143,7 +143,9 @@ def test_config1_fp32_growth_same_topology(engine32, config1):
         assert frac == 1.0 and worst <= 1, (src, t, frac, worst)
         assert [sorted(x) for x in rn.synapse_list(0)] == [sorted(x) for x in e["act"]], (src, t)
         assert [sorted(x) for x in rn.synapse_list(1)] == [sorted(x) for x in e["sup"]], (src, t)
-        np.testing.assert_allclose(rn.weights(), e["W"], rtol=1e-3, atol=1e-6)
+        # a spike one 0.02 ms step away changes that pair's LTP/LTD increment by
+        # A_P * 0.02 / T_P = 5e-6 (A_P 0.0025, T_P 10 ms): allow a few such events per weight
+        np.testing.assert_allclose(rn.weights(), e["W"], rtol=1e-3, atol=3e-5)
     rn.free()
 
 
