@@ -175,6 +175,9 @@ public:
     // [n_ra][points] (points only when out is null).
     virtual ug_status set_inhibition_tracking(double resolution, cudaStream_t st) = 0;
     virtual ug_status inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st) = 0;
+    // Brings the host copy of the per-trial bookkeeping (activity history, maturation
+    // state) up to date with the device, where growth trials keep it.
+    virtual ug_status sync_host(cudaStream_t st) = 0;
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -232,13 +235,18 @@ public:
     {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         if (ggraph_) cudaGraphExecDestroy(ggraph_);
+        if (gloop_) cudaGraphExecDestroy(gloop_);
+        if (hloop_) cudaFreeHost(hloop_);
     }
     // Group participation (ug_run_group): per-trial preparation, the member
     // descriptor, and the per-trial tail of a growth trial.
     ug_status prepare_test(uint32_t first_trial, int n_trials, cudaStream_t st);
     ug_status prepare_growth(uint32_t trial, int training, cudaStream_t st);
     ug_status member(ug::GroupMember<R>* m, int index, int2* act_rows, int* act_cnt, int act_cap, bool growth);
-    ug_status finish_growth(uint32_t trial, int bad, cudaStream_t st);
+    // The device tail of a group round's growth trial (bad: the member's check_bad_values
+    // flag on the device), then, after the round's one synchronisation, its outcome.
+    ug_status launch_finish_growth(const int* bad, cudaStream_t st);
+    ug_status complete_growth(uint32_t trial, cudaStream_t st);
     ug_status finish_test(cudaStream_t st) { return check_error(st); }
     size_t growth_row_count() const { return (size_t)h.n_ra; }
     // Device bytes this network holds now, and the bytes it will hold once
@@ -248,6 +256,7 @@ public:
     int batch() const override { return B_; }
     ug_status set_inhibition_tracking(double resolution, cudaStream_t st) override;
     ug_status inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st) override;
+    ug_status sync_host(cudaStream_t st) override { return pull_bookkeeping(st); }
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -266,7 +275,11 @@ private:
     ug_status upload_connectivity(cudaStream_t st);
     ug_status growth_init(cudaStream_t st);
     ug_status issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launches);
-    ug_status after_growth_trial(uint32_t trial, cudaStream_t st);
+    ug_status prepare_growth_run(int training, cudaStream_t st);
+    ug_status loop_outcome(uint32_t& trial, int& left, cudaStream_t st);
+    ug_status capture_growth_loop(const ug::LaunchCtx& lc);
+    ug_status push_bookkeeping(cudaStream_t st);
+    ug_status pull_bookkeeping(cudaStream_t st);
     ug_status replace_neurons(const std::vector<int>& rep, uint32_t trial, cudaStream_t st);
     ug_status sync_static_lists(cudaStream_t st);
     void drop_graphs();
@@ -294,6 +307,15 @@ private:
         gNewpostCnt_, gSomaBits_, gBad_, gRep_;
     cudaGraphExec_t ggraph_ = nullptr;
     int ggraph_training_ = -1;
+    // per-trial bookkeeping on the device (ug_tail.cuh): allocated once by growth_init,
+    // refreshed in place, so graphs captured with their addresses stay valid
+    DevMem gHist_, gHead_, gHsum_, gHact_, gFrl_, gScale_, gMatf_, gRest_, gGca_, gMature_, gTar_, gRepCnt_, gLoop_;
+    ug::TailDev<R> td_{};
+    bool book_dirty_ = false;      // the device bookkeeping changed since the host copy was read
+    int* hloop_ = nullptr;         // pinned copy of the loop words
+    cudaGraphExec_t gloop_ = nullptr;   // the multi-trial loop: a WHILE node around one growth trial
+    int gloop_training_ = -1;
+    int gloop_ginh_gen_ = -1;
     // inhibition tracking
     double ginh_res_ = 0.0;
     int ginh_points_ = 0;
@@ -531,6 +553,9 @@ void NetImpl<R>::drop_graphs()
     if (ggraph_) cudaGraphExecDestroy(ggraph_);
     ggraph_ = nullptr;
     ggraph_training_ = -1;
+    if (gloop_) cudaGraphExecDestroy(gloop_);
+    gloop_ = nullptr;
+    gloop_training_ = -1;
 }
 
 template <class R>
@@ -647,7 +672,9 @@ size_t NetImpl<R>::device_bytes() const
         t += m->bytes();
     for (const DevMem* m : {&gW_, &gD_, &gPerm_, &gActive_, &gSuper_, &gActList_, &gActCnt_, &gSupList_, &gSupCnt_,
                             &gRemod_, &gPreStep_, &gPreCnt_, &gPostStep_, &gPostCnt_, &gPostLast_, &gSpikeLast_, &gStStep_, &gStCur_, &gStLen_,
-                            &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_})
+                            &gStTgt_, &gStHead_, &gStNum_, &gNewpost_, &gNewpostCnt_, &gSomaBits_, &gBad_, &gRep_,
+                            &gHist_, &gHead_, &gHsum_, &gHact_, &gFrl_, &gScale_, &gMatf_, &gRest_, &gGca_, &gMature_,
+                            &gTar_, &gRepCnt_, &gLoop_})
         t += m->bytes();
     return t;
 }
@@ -671,6 +698,8 @@ size_t NetImpl<R>::footprint(int kind, int B) const
         const size_t nn = nra * nra;
         t += 35 * nn + nra * (4 + 4 * ug::kMaxNss + 12 + 4 * ug::kPostRing + 4 + 16 + 3 * 4 * ug::kMaxStreams +
                               4 * ug::kMaxStreams * ug::kMaxNss + 8 + 64 + 8 + 4 + 4) + 8;
+        // per-trial bookkeeping (activity history ring, maturation state)
+        t += nra * (4 * (size_t)std::max(h.mat.RATE_WINDOW_LONG, 0) + 8 + 4 + 5 * 8 + 4 + 4) + 32;
     }
     return t;
 }
@@ -856,7 +885,93 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     g.st_tgt = gStTgt_.as<int>(); g.st_head = gStHead_.as<int>(); g.st_num = gStNum_.as<int>();
     g.newpost = gNewpost_.as<int>(); g.newpost_cnt = gNewpostCnt_.as<int>();
     g.error = error_.as<int>();
+
+    // per-trial bookkeeping on the device
+    const int win = h.mat.RATE_WINDOW_LONG;
+    UG_TRY(gHist_.alloc((size_t)n * win * sizeof(int)));
+    UG_TRY(gHead_.alloc(sizeof(int)));
+    UG_TRY(gHsum_.alloc((size_t)n * sizeof(long long)));
+    UG_TRY(gHact_.alloc((size_t)n * sizeof(int)));
+    for (DevMem* m : {&gFrl_, &gScale_, &gMatf_, &gRest_, &gGca_}) UG_TRY(m->alloc((size_t)n * sizeof(double)));
+    UG_TRY(gMature_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gTar_.alloc((size_t)n * sizeof(int)));
+    UG_TRY(gRepCnt_.alloc(sizeof(int)));
+    UG_TRY(gLoop_.alloc(ug::kLoopWords * sizeof(int)));
+    if (!hloop_) UG_CUDA(cudaMallocHost(&hloop_, ug::kLoopWords * sizeof(int)));
+    ug::TailDev<R>& t = td_;
+    t.n = n;
+    t.W = win;
+    t.nsoma = ra_nsoma_.as<int>();   // set again by prepare_growth_run once the batch exists
+    t.hist = gHist_.as<int>(); t.head = gHead_.as<int>(); t.hsum = gHsum_.as<long long>(); t.hact = gHact_.as<int>();
+    t.frl = gFrl_.as<double>(); t.scale = gScale_.as<double>(); t.matf = gMatf_.as<double>();
+    t.rest = gRest_.as<double>(); t.gca = gGca_.as<double>(); t.mature = gMature_.as<int>(); t.tar = gTar_.as<int>();
+    t.Erest = dErest_.as<R>(); t.GCa = dGCa_.as<R>();
+    t.rep = gRep_.as<int>(); t.rep_cnt = gRepCnt_.as<int>();
+    t.bad = gBad_.as<int>(); t.error = error_.as<int>(); t.loop = gLoop_.as<int>();
+    t.e_rest_mature = h.mat.E_REST_MATURE; t.gca_mature = h.mat.GCA_MATURE;
+    t.death_rate = h.mat.DEATH_RATE_THRESHOLD;
+    t.matf_driven = std::exp(-1.0 / 1000.0) - 1;   // MATURATION_SCALE_DRIVEN
+    t.seed = h.seed; t.net_id = (uint32_t)h.net_id;
+    t.has_cond = 0;
+    UG_TRY(push_bookkeeping(st));
     growth_ready_ = true;
+    return UG_OK;
+}
+
+// Host copy of the per-trial bookkeeping -> device (in place: the loop graph holds the
+// addresses).  exp(-1 / scale) - 1 is taken here, with the host's exponential.
+template <class R>
+ug_status NetImpl<R>::push_bookkeeping(cudaStream_t st)
+{
+    const int n = h.n_ra;
+    std::vector<double> matf(n);
+    for (int i = 0; i < n; ++i) matf[i] = std::exp(-1.0 / h.scale[i]) - 1;
+    std::vector<R> er(h.rest.begin(), h.rest.end()), gc(h.gca.begin(), h.gca.end());
+    auto put = [&](DevMem& m, const void* src, size_t bytes) -> ug_status {
+        if (bytes > m.bytes()) return fail(UG_EINVAL, "bookkeeping array larger than its allocation");
+        if (bytes) UG_CUDA(cudaMemcpyAsync(m.as<void>(), src, bytes, cudaMemcpyHostToDevice, st));
+        return UG_OK;
+    };
+    UG_TRY(put(gHist_, h.hist.data(), h.hist.size() * sizeof(int)));
+    UG_TRY(put(gHead_, &h.hist_head, sizeof(int)));
+    UG_TRY(put(gHsum_, h.hist_sum.data(), (size_t)n * sizeof(long long)));
+    UG_TRY(put(gHact_, h.hist_active.data(), (size_t)n * sizeof(int)));
+    UG_TRY(put(gFrl_, h.frl.data(), (size_t)n * sizeof(double)));
+    UG_TRY(put(gScale_, h.scale.data(), (size_t)n * sizeof(double)));
+    UG_TRY(put(gMatf_, matf.data(), (size_t)n * sizeof(double)));
+    UG_TRY(put(gRest_, h.rest.data(), (size_t)n * sizeof(double)));
+    UG_TRY(put(gGca_, h.gca.data(), (size_t)n * sizeof(double)));
+    UG_TRY(put(gMature_, h.mature.data(), (size_t)n * sizeof(int)));
+    UG_TRY(put(gTar_, h.tar.data(), (size_t)n * sizeof(int)));
+    UG_TRY(put(dErest_, er.data(), (size_t)n * sizeof(R)));
+    UG_TRY(put(dGCa_, gc.data(), (size_t)n * sizeof(R)));
+    UG_CUDA(cudaStreamSynchronize(st));   // the host vectors above are temporaries
+    book_dirty_ = false;
+    return UG_OK;
+}
+
+// Device bookkeeping -> host copy (getters, files, replacement), when it changed.
+template <class R>
+ug_status NetImpl<R>::pull_bookkeeping(cudaStream_t st)
+{
+    if (!book_dirty_) return UG_OK;
+    const int n = h.n_ra;
+    UG_CUDA(cudaStreamSynchronize(st));
+    auto get = [&](void* dst, const DevMem& m, size_t bytes) -> ug_status {
+        if (bytes) UG_CUDA(cudaMemcpy(dst, m.as<void>(), bytes, cudaMemcpyDeviceToHost));
+        return UG_OK;
+    };
+    UG_TRY(get(h.hist.data(), gHist_, h.hist.size() * sizeof(int)));
+    UG_TRY(get(&h.hist_head, gHead_, sizeof(int)));
+    UG_TRY(get(h.hist_sum.data(), gHsum_, (size_t)n * sizeof(long long)));
+    UG_TRY(get(h.hist_active.data(), gHact_, (size_t)n * sizeof(int)));
+    UG_TRY(get(h.frl.data(), gFrl_, (size_t)n * sizeof(double)));
+    UG_TRY(get(h.scale.data(), gScale_, (size_t)n * sizeof(double)));
+    UG_TRY(get(h.rest.data(), gRest_, (size_t)n * sizeof(double)));
+    UG_TRY(get(h.gca.data(), gGca_, (size_t)n * sizeof(double)));
+    UG_TRY(get(h.mature.data(), gMature_, (size_t)n * sizeof(int)));
+    UG_TRY(get(h.tar.data(), gTar_, (size_t)n * sizeof(int)));
+    book_dirty_ = false;
     return UG_OK;
 }
 
@@ -884,53 +999,153 @@ ug_status NetImpl<R>::issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launc
     return UG_OK;
 }
 
+// Consecutive growth trials.  With graphs, one launch runs them all: a WHILE node
+// around one trial (k_growth_head, the trial's kernels, check_bad_values, k_growth_tail),
+// whose condition the tail clears when the trials are done, a neuron must be replaced or
+// the trial failed.  The host then reads the loop words once; a replacement (rare) is
+// done on the host and the loop resumes with the next trial.
 template <class R>
 ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int training, const ug::LaunchCtx& lc,
                                         bool graphs, int64_t* launches)
 {
     cudaStream_t st = lc.main;
     if (n_trials <= 0) return fail(UG_EINVAL, "n_trials must be positive");
-    for (int t = 0; t < n_trials; ++t) {
-        const uint32_t trial = first_trial + (uint32_t)t;
-        UG_TRY(prepare_growth(trial, training, st));
-        if (!graphs || lc.timer) {
-            UG_TRY(issue_growth_trial(lc, launches));
+    UG_TRY(prepare_growth_run(training, st));
+    uint32_t trial = first_trial;
+    int left = n_trials;
+    const int64_t per_trial = 2 + (sizeof(R) == 4 ? 1 : 0) + 5 * (int64_t)sync_steps.size() + 2 + 3;
+    while (left > 0) {
+        const int words[ug::kLoopWords] = {left, (int)trial, ug::kLoopRunning, 0};
+        UG_CUDA(cudaMemcpyAsync(gLoop_.as<int>(), words, sizeof(words), cudaMemcpyHostToDevice, st));
+        if (graphs && !lc.timer) {
+            if (!gloop_ || gloop_training_ != bd_.kick_on || gloop_ginh_gen_ != ginh_gen_) UG_TRY(capture_growth_loop(lc));
+            UG_CUDA(cudaGraphLaunch(gloop_, st));
+            UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost, st));
+            UG_CUDA(cudaStreamSynchronize(st));
         } else {
-            if (!ggraph_ || ggraph_training_ != bd_.kick_on || ggraph_ginh_gen_ != ginh_gen_) {
-                if (ggraph_) cudaGraphExecDestroy(ggraph_);
-                ggraph_ = nullptr;
-                cudaStream_t cap;
-                UG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
-                cudaGraph_t g;
-                UG_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
-                ug::LaunchCtx clc = lc;
-                clc.main = cap;
-                int64_t dummy = 0;
-                ug_status s = issue_growth_trial(clc, &dummy);
-                cudaError_t e = cudaStreamEndCapture(cap, &g);
-                cudaStreamDestroy(cap);
-                if (s != UG_OK) return s;
-                UG_CUDA(e);
-                e = cudaGraphInstantiate(&ggraph_, g, 0);
-                cudaGraphDestroy(g);
-                UG_CUDA(e);
-                ggraph_training_ = bd_.kick_on;
-                ggraph_ginh_gen_ = ginh_gen_;
+            // one trial at a time, the host reading the loop words after each
+            for (;;) {
+                ug::TailDev<R> t = td_;
+                t.has_cond = 0;
+                UG_CUDA(ug::launch_growth_head<R>(t, gBad_.as<int>(), st));
+                UG_TRY(issue_growth_trial(lc, launches));
+                UG_CUDA(ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), st));
+                UG_CUDA(ug::launch_growth_tail<R>(t, st));
+                UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost,
+                                        st));
+                UG_CUDA(cudaStreamSynchronize(st));
+                if (hloop_[ug::kLoopStatus] != ug::kLoopRunning || hloop_[ug::kLoopRemaining] <= 0) break;
             }
-            UG_CUDA(cudaGraphLaunch(ggraph_, st));
-            int64_t n = 0;
-            ug::LaunchCtx none;
-            (void)none;
-            n = 3 + (sizeof(R) == 4 ? 1 : 0) + 5 * (int64_t)sync_steps.size() + 2;
-            if (launches) *launches += n;
         }
-        // check_bad_values after the trial (:5794-5803)
-        UG_CUDA(cudaMemsetAsync(gBad_.as<int>(), 0, sizeof(int), st));
-        UG_CUDA(ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), st));
-        int bad = 0;
-        UG_CUDA(cudaMemcpyAsync(&bad, gBad_.as<int>(), sizeof(int), cudaMemcpyDeviceToHost, st));
-        UG_TRY(finish_growth(trial, bad, st));
+        if (launches) *launches += per_trial * std::max(hloop_[ug::kLoopDone], 1);
+        UG_TRY(loop_outcome(trial, left, st));
     }
+    return UG_OK;
+}
+
+// The loop words after a run: trials done, and the reason it stopped.
+template <class R>
+ug_status NetImpl<R>::loop_outcome(uint32_t& trial, int& left, cudaStream_t st)
+{
+    const int done = hloop_[ug::kLoopDone], status = hloop_[ug::kLoopStatus];
+    rara_dirty_ = true;
+    book_dirty_ = true;
+    if (status == ug::kLoopBad) return fail(UG_ENUMERIC, "bad values in the neuron dynamics (check_bad_values)");
+    if (status == ug::kLoopCapacity) {
+        UG_TRY(check_error(st));
+        return fail(UG_ECAPACITY, "device event buffer overflowed");
+    }
+    trial += (uint32_t)done;
+    left -= done;
+    replaced.clear();
+    if (status == ug::kLoopReplace) {
+        // replace_neurons (:15869-15881) after the trial that found them
+        int cnt = 0;
+        UG_CUDA(cudaMemcpy(&cnt, gRepCnt_.as<int>(), sizeof(int), cudaMemcpyDeviceToHost));
+        std::vector<int> rep(cnt);
+        if (cnt) UG_CUDA(cudaMemcpy(rep.data(), gRep_.as<int>(), cnt * sizeof(int), cudaMemcpyDeviceToHost));
+        UG_TRY(pull_bookkeeping(st));
+        replaced = rep;
+        UG_TRY(replace_neurons(rep, trial - 1, st));
+        UG_TRY(push_bookkeeping(st));
+    }
+    return UG_OK;
+}
+
+// The loop graph: WHILE (condition set by k_growth_tail) { head; trial; check; tail }.
+template <class R>
+ug_status NetImpl<R>::capture_growth_loop(const ug::LaunchCtx& lc)
+{
+    if (gloop_) cudaGraphExecDestroy(gloop_);
+    gloop_ = nullptr;
+    cudaGraph_t g = nullptr;
+    UG_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle cond;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&cond, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams p = {};
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) {
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = cond;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+    }
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        UG_CUDA(e);
+    }
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    cudaStream_t cap;
+    e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        UG_CUDA(e);
+    }
+    e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    ug_status s = UG_OK;
+    if (e == cudaSuccess) {
+        ug::LaunchCtx clc = lc;
+        clc.main = cap;
+        ug::TailDev<R> t = td_;
+        t.cond = cond;
+        t.has_cond = 1;
+        int64_t dummy = 0;
+        e = ug::launch_growth_head<R>(t, gBad_.as<int>(), cap);
+        if (e == cudaSuccess) s = issue_growth_trial(clc, &dummy);
+        if (e == cudaSuccess && s == UG_OK) e = ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), cap);
+        if (e == cudaSuccess && s == UG_OK) e = ug::launch_growth_tail<R>(t, cap);
+        cudaGraph_t out = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(cap, &out);
+        if (e == cudaSuccess) e = e2;
+    }
+    cudaStreamDestroy(cap);
+    if (s == UG_OK && e == cudaSuccess) e = cudaGraphInstantiate(&gloop_, g, 0);
+    cudaGraphDestroy(g);
+    if (s != UG_OK) return s;
+    UG_CUDA(e);
+    gloop_training_ = bd_.kick_on;
+    gloop_ginh_gen_ = ginh_gen_;
+    return UG_OK;
+}
+
+// Per-run settings of single-network growth trials (instance 0 of a batch of one).
+template <class R>
+ug_status NetImpl<R>::prepare_growth_run(int training, cudaStream_t st)
+{
+    if (!growth_ready_) UG_TRY(growth_init(st));
+    UG_TRY(ensure_batch(1));
+    bd_.B = 1;
+    bd_.kick_on = training ? 1 : 0;
+    bd_.scatter_rara = 0;
+    bd_.soma_bits = gSomaBits_.as<int>();
+    bd_.ginh_rec = ginh_res_ > 0 ? gGinh_.as<R>() : nullptr;
+    bd_.ginh_slot = ginh_res_ > 0 ? gGinhSlot_.as<int>() : nullptr;
+    if (ginh_res_ > 0) ginh_recorded_ = true;
+    B_ = 1;
+    td_.nsoma = ra_nsoma_.as<int>();
+    td_.trial_dev = trial_.as<uint32_t>();
+    td_.mean_inj = mean_inj_.as<double>();
     return UG_OK;
 }
 
@@ -947,13 +1162,18 @@ ug_status NetImpl<R>::prepare_growth(uint32_t trial, int training, cudaStream_t 
     bd_.ginh_slot = ginh_res_ > 0 ? gGinhSlot_.as<int>() : nullptr;
     if (ginh_res_ > 0) ginh_recorded_ = true;
     B_ = 1;
+    td_.nsoma = ra_nsoma_.as<int>();
+    td_.trial_dev = trial_.as<uint32_t>();
+    td_.mean_inj = mean_inj_.as<double>();
     UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
-    // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901)
+    // mean training injection time: WAITING_TIME + random(TRIAL_DURATION - 2 WAITING_TIME) (:8894-8901).
+    // Copies from pageable memory return once the source is staged, so no synchronisation.
     ug::HostStream hs{ug::make_stream(h.seed, ug::kNoiseTrial, (uint32_t)h.net_id, 0, trial), 0};
     const double mean_inj = 100.0 + ug::random_G(300.0, hs.word());
+    const int words[ug::kLoopWords] = {1, (int)trial, ug::kLoopRunning, 0};
     UG_CUDA(cudaMemcpyAsync(trial_.as<uint32_t>(), &trial, sizeof(uint32_t), cudaMemcpyHostToDevice, st));
     UG_CUDA(cudaMemcpyAsync(mean_inj_.as<double>(), &mean_inj, sizeof(double), cudaMemcpyHostToDevice, st));
-    UG_CUDA(cudaStreamSynchronize(st));
+    UG_CUDA(cudaMemcpyAsync(gLoop_.as<int>(), words, sizeof(words), cudaMemcpyHostToDevice, st));
     return UG_OK;
 }
 
@@ -1014,14 +1234,24 @@ ug_status NetImpl<R>::inhibition(double* out, int32_t* points, double* resolutio
     return UG_OK;
 }
 
-// bad: the check_bad_values flag of the trial (read back by the caller's stream).
+// The device tail of a group round's growth trial, and an asynchronous read of its
+// loop words; the round synchronises once for every member.
 template <class R>
-ug_status NetImpl<R>::finish_growth(uint32_t trial, int bad, cudaStream_t st)
+ug_status NetImpl<R>::launch_finish_growth(const int* bad, cudaStream_t st)
 {
-    UG_TRY(check_error(st));
-    if (bad) return fail(UG_ENUMERIC, "bad values in the neuron dynamics (check_bad_values)");
-    rara_dirty_ = true;
-    return after_growth_trial(trial, st);
+    ug::TailDev<R> t = td_;
+    t.bad = bad;
+    t.has_cond = 0;
+    UG_CUDA(ug::launch_growth_tail<R>(t, st));
+    UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost, st));
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::complete_growth(uint32_t trial, cudaStream_t st)
+{
+    int left = 1;
+    return loop_outcome(trial, left, st);
 }
 
 // Descriptor of this network as member `index` of a group.  Growth members
@@ -1061,56 +1291,6 @@ ug_status NetImpl<R>::member(ug::GroupMember<R>* m, int index, int2* act_rows, i
             m->bt.heavy = (double)h.n_ra * 0.25 / delay_spread_ > 256.0 ? 2 : 1;
         }
     }
-    return UG_OK;
-}
-
-// The per-trial tail of chain_growth (NetworkGrowthSimulator.cpp:5841-5875):
-// trial counters, check_neuron_activity (:9573-9627), maturation
-// (update_neuron_properties_sameDendrite_diffMaturationRate, :2152-2183),
-// replacement (:15869-15881).  The next trial starts from set_to_rest.
-template <class R>
-ug_status NetImpl<R>::after_growth_trial(uint32_t trial, cudaStream_t st)
-{
-    const int n = h.n_ra;
-    const int W = h.mat.RATE_WINDOW_LONG;
-    std::vector<int> count(n);
-    UG_CUDA(cudaMemcpyAsync(count.data(), ra_nsoma_.as<int>(), n * sizeof(int), cudaMemcpyDeviceToHost, st));
-    UG_CUDA(cudaStreamSynchronize(st));
-    for (int i = 0; i < n; ++i) h.tar[i] += 1;
-    std::vector<int> rep;
-    // push_front into the full circular buffer: the new count takes the slot of
-    // the oldest, and the 1000th newest leaves the robustness window (the sums
-    // are integers, so the rates equal the reference's full re-summation)
-    const int head = (h.hist_head + W - 1) % W;
-    const int leave = (h.hist_head + 999) % W;
-    for (int i = 0; i < n; ++i) {
-        int* hi = h.hist.data() + (size_t)i * W;
-        const int oldest = hi[head], leaving = hi[leave];
-        hi[head] = count[i];
-        h.hist_sum[i] += count[i] - oldest;
-        h.hist_active[i] += (count[i] > 0 ? 1 : 0) - (leaving > 0 ? 1 : 0);
-        h.frl[i] = (double)h.hist_sum[i] / (double)W;
-        const double robust = (double)h.hist_active[i] / 1000.0;
-        if (robust >= 0.5 && h.scale[i] != 1000.0) h.scale[i] = 1000.0;   // MATURATION_SCALE_DRIVEN
-        if (robust < h.mat.DEATH_RATE_THRESHOLD && h.tar[i] > 1000) rep.push_back(i);
-    }
-    h.hist_head = head;
-    for (int i = 0; i < n; ++i) {
-        if (h.mature[i] == 1) continue;
-        h.rest[i] = h.rest[i] + (h.rest[i] - h.mat.E_REST_MATURE) * (std::exp(-1.0 / h.scale[i]) - 1);
-        h.gca[i] = h.gca[i] + (h.gca[i] - h.mat.GCA_MATURE) * (std::exp(-1.0 / h.scale[i]) - 1);
-        if ((h.gca[i] >= h.mat.GCA_MATURE - 0.5) || (h.rest[i] <= h.mat.E_REST_MATURE - 0.5)) {
-            h.gca[i] = h.mat.GCA_MATURE;
-            h.rest[i] = h.mat.E_REST_MATURE;
-            h.mature[i] = 1;
-        }
-    }
-    replaced = rep;
-    if (!rep.empty()) UG_TRY(replace_neurons(rep, trial, st));
-    std::vector<R> er(h.rest.begin(), h.rest.end()), gc(h.gca.begin(), h.gca.end());
-    UG_CUDA(cudaMemcpyAsync(dErest_.as<R>(), er.data(), n * sizeof(R), cudaMemcpyHostToDevice, st));
-    UG_CUDA(cudaMemcpyAsync(dGCa_.as<R>(), gc.data(), n * sizeof(R), cudaMemcpyHostToDevice, st));
-    UG_CUDA(cudaStreamSynchronize(st));
     return UG_OK;
 }
 
@@ -1299,6 +1479,7 @@ ug_status NetImpl<R>::neuron_props(double* rest, double* gca, int32_t* mature, d
                                    int32_t* tar, double* frl, cudaStream_t st)
 {
     if (rara_dirty_) UG_TRY(sync_static_lists(st));
+    UG_TRY(pull_bookkeeping(st));
     for (int i = 0; i < h.n_ra; ++i) {
         if (rest) rest[i] = h.rest[i];
         if (gca) gca[i] = h.gca[i];
@@ -1500,13 +1681,14 @@ ug_status GroupExec<R>::run_round(std::vector<RoundItem<R>>& items, const ug::La
         UG_CUDA(cudaGraphLaunch(ge, st));
     }
     if (launches) *launches += n_launch;
-    hbad_.assign(M, 0);
-    UG_CUDA(cudaMemcpyAsync(hbad_.data(), bad_.as<int>(), (size_t)M * sizeof(int), cudaMemcpyDeviceToHost, st));
+    // the device tails of the growth members, then one synchronisation for the round
+    for (int m = 0; m < M; ++m)
+        if (items[m].kind == 1) UG_TRY(items[m].net->launch_finish_growth(bad_.as<int>() + m, st));
     UG_CUDA(cudaStreamSynchronize(st));
     ug_status first = UG_OK;
     for (int m = 0; m < M; ++m) {
         RoundItem<R>& it = items[m];
-        it.status = it.kind == 1 ? it.net->finish_growth(it.trial, hbad_[m], st) : it.net->finish_test(st);
+        it.status = it.kind == 1 ? it.net->complete_growth(it.trial, st) : it.net->finish_test(st);
         if (it.status != UG_OK && first == UG_OK) first = it.status;
     }
     return first;
@@ -2190,6 +2372,7 @@ ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out)
     NetBase* n;
     UG_TRY(get_net(ctx, net_id, &n));
     if (!out) return fail(UG_EINVAL, "null output");
+    UG_TRY(n->sync_host(ctx->stream));
     const int W = n->h.mat.RATE_WINDOW_LONG;
     if (W <= 0) return UG_OK;
     for (int i = 0; i < n->h.n_ra; ++i)

@@ -168,6 +168,20 @@ cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad,
     return cudaGetLastError();
 }
 
+template <class R>
+cudaError_t launch_growth_head(const TailDev<R>& t, int* bad, cudaStream_t st)
+{
+    k_growth_head<R><<<1, 1, 0, st>>>(t, bad);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t launch_growth_tail(const TailDev<R>& t, cudaStream_t st)
+{
+    k_growth_tail<R><<<1, kTailThreads, 0, st>>>(t);
+    return cudaGetLastError();
+}
+
 template <class K>
 static int occupancy(K kernel, int threads, size_t smem)
 {

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ug_group.cuh"
+#include "ug_tail.cuh"
 
 namespace ug {
 
@@ -126,6 +127,11 @@ template <class R>
 cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st);
 template <class R>
 cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad, cudaStream_t st);
+// The device tail of a growth trial and the head of the next (ug_tail.cuh).
+template <class R>
+cudaError_t launch_growth_head(const TailDev<R>& t, int* bad, cudaStream_t st);
+template <class R>
+cudaError_t launch_growth_tail(const TailDev<R>& t, cudaStream_t st);
 
 // Group launches (ug_group.cuh): the work lists and row queue of a group, in
 // device memory, and the fixed grid of each list kernel.
