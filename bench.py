@@ -37,9 +37,10 @@ SEED = 3
 # Work per neuron-step of the single-precision integrators, counted from their
 # source (csrc/ug_ra_f32x2.cuh, csrc/ug_i_f32.cuh): FP32 lane operations (a packed
 # f32x2 operation counts 2) and SFU operations (ex2, rcp).
-#   RA: 4 stages x 90 packed ops + 128 packed ops of stage sums  = 488 FP32 ops; 4 x (8 ex2 + 2 rcp) = 40 SFU
+#   RA: 4 stages x 82 packed ops + 122 packed ops of stage sums and noise = 450 FP32 ops;
+#       4 x (8 ex2 + 2 rcp) = 40 SFU
 #   I : 12 stages x 63 ops + 376 ops of the DP8 tableau sums      = 1132 FP32 ops; 12 x (4 ex2 + 1 rcp) = 60 SFU
-FP32_RA, FP32_I = 488, 1132
+FP32_RA, FP32_I = 450, 1132
 MUFU_RA, MUFU_I = 40, 60
 # DRAM bytes per launch of the dominant kernel from an ncu capture of the integrators
 # at 128 trials (16.4 MB read, ~0 written), scaled to a launch of BATCH trials: the state

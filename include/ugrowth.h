@@ -234,6 +234,27 @@ ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out);
 /* Training neurons and their spread times, [n_tr] each. */
 ug_status ug_get_training(ug_ctx* ctx, int32_t net_id, int32_t* neurons, double* spread);
 
+/* ---- Per-neuron traces (set_recording, NetworkGrowthSimulator.cpp:2352-2407) -------------
+ * The listed neurons (at most 1024 of each kind) record their state before every step of
+ * the next trials -- test trials (instance 0 of the batch) and growth trials of this
+ * network run alone (group members do not record) -- as HH2_test::record_state and
+ * HHI_buffer::record_state keep it (HH2_test.cpp:476-497, HHI_buffer.cpp:148-167).  Empty
+ * lists switch recording off. */
+ug_status ug_set_recording(ug_ctx* ctx, int32_t net_id, const int32_t* ra_ids, int32_t n_ra_ids, const int32_t* i_ids,
+                           int32_t n_i_ids);
+ug_status ug_get_recording(ug_ctx* ctx, int32_t net_id, int32_t* ra_ids, int32_t* n_ra_ids, int32_t* i_ids,
+                           int32_t* n_i_ids);
+/* The last trial's trace of the k-th recorded neuron of a kind (which 0 HVC(RA), 1 HVC(I)):
+ * n_records = num_steps - 1 rows, one per step, each the time before the step and the
+ * state then -- HVC(RA): time, Vs, Vd, Gexc_d, Ginh_d; HVC(I): time, V, Gexc, Ginh.
+ * out may be NULL to query n_records. */
+ug_status ug_get_trace(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t k, double* out, int32_t* n_records);
+/* The reference's trace files of the last trial: <dir>/RA/RA<id>_trial<trial_number>.bin and
+ * <dir>/I/I<id>_trial<trial_number>.bin, records of the layout above, whole buffers of 1000
+ * records only (HH2_test::write_buffers, HH2_test.cpp:394-411; HHI_buffer::write_buffers,
+ * HHI_buffer.cpp:720-734: a trial's last partial buffer is not written). */
+ug_status ug_write_traces(ug_ctx* ctx, int32_t net_id, const char* dir, int32_t trial_number);
+
 /* Reference directory formats.  read_network_state (NetworkGrowthSimulator.cpp:1943-2020):
  * loads the state files of `dir` for `starting_trial` ("_<trial>" suffix when > 0) and its
  * growth_parameters.cfg / network_parameters.cfg; num_steps 0 means 25000 (a 500 ms trial).
@@ -392,6 +413,14 @@ ug_status ug_create_network_topology(ug_ctx* ctx, const char* config_file, const
  * SFU (ex2/rcp approximations, operations per second) and of FP32 FMA on `device`,
  * the denominators of the integrators' roofline. */
 ug_status ug_calibrate_pipes(int32_t device, double* mufu_ops_per_s, double* fma_ops_per_s);
+
+/* No counterpart in the reference (failure detection).  Every wait in the library's kernels
+ * (on an mbarrier of the bulk copy engine, or on a flag in global memory) gives up after
+ * one second and raises UG_ETIMEOUT instead of hanging the device.  This runs one such wait
+ * that nothing can satisfy -- which 0: a global flag nothing sets; which 1: an mbarrier
+ * expecting bytes no copy delivers -- and returns UG_ETIMEOUT once it gives up; the device
+ * stays usable. */
+ug_status ug_probe_bounded_wait(int32_t device, int32_t which);
 
 #ifdef __cplusplus
 }

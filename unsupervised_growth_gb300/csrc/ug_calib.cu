@@ -3,6 +3,7 @@
 // FMA pipe.  Each thread runs 8 independent dependency chains so the
 // measurement is throughput-, not latency-bound; grid = 4 x SM count blocks.
 #include "ugrowth.h"
+#include "ug_async.cuh"
 #include <cuda_runtime.h>
 #include <string>
 
@@ -51,7 +52,46 @@ __global__ void k_fma_loop(float* out, int iters, float seed)
     if (s == 12345.678f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// A wait that nothing can satisfy, bounded like every wait of the library: which 0 polls
+// a global flag nothing sets; which 1 waits on an mbarrier that expects 16 bytes of
+// transactions no copy delivers.  error[0] gets 8 (the timeout flag) once it gives up.
+__global__ void k_wait_probe(int which, const int* flag, int* error)
+{
+    __shared__ uint64_t bar;
+    bool ok;
+    if (which == 0) {
+        ok = ug::flag_wait_bounded(flag);
+    } else {
+        if (threadIdx.x == 0) {
+            ug::mbar_init(&bar, 1);
+            ug::fence_mbar_init();
+            ug::mbar_arrive_expect_tx(&bar, 16);
+        }
+        __syncthreads();
+        ok = ug::mbar_wait_bounded(&bar, 0);
+    }
+    if (!ok && threadIdx.x == 0) atomicOr(error, 8);
+}
+
 }  // namespace
+
+extern "C" ug_status ug_probe_bounded_wait(int32_t device, int32_t which)
+{
+    if (which != 0 && which != 1) return UG_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return UG_ECUDA;
+    int* buf = nullptr;
+    if (cudaMalloc(&buf, 2 * sizeof(int)) != cudaSuccess) return UG_ENOMEM;
+    int host[2] = {0, 0};
+    cudaError_t e = cudaMemset(buf, 0, 2 * sizeof(int));
+    if (e == cudaSuccess) {
+        k_wait_probe<<<1, 32>>>(which, buf, buf + 1);
+        e = cudaDeviceSynchronize();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(host, buf, sizeof(host), cudaMemcpyDeviceToHost);
+    cudaFree(buf);
+    if (e != cudaSuccess) return UG_ECUDA;
+    return host[1] & 8 ? UG_ETIMEOUT : UG_OK;
+}
 
 extern "C" ug_status ug_calibrate_pipes(int32_t device, double* mufu_ops_per_s, double* fma_ops_per_s)
 {

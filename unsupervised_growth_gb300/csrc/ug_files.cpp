@@ -10,8 +10,11 @@
 #include "ug_philox.cuh"
 #include "ug_topology.h"
 
+#include <sys/stat.h>
+
 #include <algorithm>
 #include <cctype>
+#include <cerrno>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -715,6 +718,42 @@ ug_status ug_write_jitter(ug_ctx* ctx, int32_t net, const char* path)
         }
     }
     return closed(o, path);
+}
+
+// set_recording's files (NetworkGrowthSimulator.cpp:2352-2407): per recorded neuron,
+// RA/RA<id>_trial<t>.bin or I/I<id>_trial<t>.bin of (time, state) records of doubles, in
+// whole buffers of 1000 records as write_buffers appends them (HH2_test.cpp:394-411,
+// HHI_buffer.cpp:720-734); the trial's last partial buffer is never written.
+ug_status ug_write_traces(ug_ctx* ctx, int32_t net, const char* dir, int32_t trial_number)
+{
+    if (!ctx || !dir) return ferr(UG_EINVAL, "null argument");
+    int32_t nra = 0, ni = 0;
+    UG_FTRY(ug_get_recording(ctx, net, nullptr, &nra, nullptr, &ni));
+    std::vector<int32_t> ra((size_t)std::max(nra, 1)), in((size_t)std::max(ni, 1));
+    UG_FTRY(ug_get_recording(ctx, net, ra.data(), &nra, in.data(), &ni));
+    const int kBuffer = 1000;   // HH2_test::BUFFER_SIZE, HHI_buffer's likewise
+    for (int which = 0; which < 2; ++which) {
+        const int cnt = which == 0 ? nra : ni;
+        if (cnt == 0) continue;
+        const std::string sub = join(dir, which == 0 ? "RA" : "I");
+        if (::mkdir(sub.c_str(), 0755) != 0 && errno != EEXIST) return ferr(UG_EIO, "cannot create " + sub);
+        for (int k = 0; k < cnt; ++k) {
+            int32_t records = 0;
+            UG_FTRY(ug_get_trace(ctx, net, which, k, nullptr, &records));
+            const int w = which == 0 ? 5 : 4;
+            std::vector<double> rec((size_t)records * w);
+            UG_FTRY(ug_get_trace(ctx, net, which, k, rec.data(), &records));
+            const int id = which == 0 ? ra[k] : in[k];
+            const std::string path = join(sub, std::string(which == 0 ? "RA" : "I") + std::to_string(id) + "_trial" +
+                                                   std::to_string(trial_number) + ".bin");
+            Out o(path, false);
+            const size_t whole = (size_t)(records / kBuffer) * kBuffer;
+            for (size_t r = 0; r < whole; ++r)
+                for (int c = 0; c < w; ++c) o.put(rec[r * w + c]);
+            UG_FTRY(closed(o, path));
+        }
+    }
+    return UG_OK;
 }
 
 ug_status ug_write_spike_times(ug_ctx* ctx, int32_t net, int32_t instance, int32_t which, const char* path,

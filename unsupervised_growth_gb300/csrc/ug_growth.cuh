@@ -24,6 +24,7 @@
 // gated 30 ms apart, so only the last 4 can fall inside the 100 ms STDP window:
 // small rings replace the reference's unbounded vectors.
 #pragma once
+#include "ug_async.cuh"
 #include "ug_trial.cuh"
 
 namespace ug {
@@ -38,6 +39,11 @@ struct SynParams {
     int Nss;
     double A_P, A_D, T_0, T_P, T_D, TAU_P, TAU_D, BETA, BETA_SUPERSYNAPSE;
     double ACTIVATION_THRESHOLD, SUPERSYNAPSE_THRESHOLD, WEIGHT_MAX;
+    // Both thresholds positive: the epilogue compares weights with them as bit patterns
+    // (a double's bits order like an int64 for values >= +0; every other weight is below
+    // both thresholds either way), so its only floating-point operation is the decay.
+    int int_thresholds;
+    long long act_bits, sup_bits;   // the thresholds' bit patterns
 };
 
 // Device state of the RA->RA synapses of B growing networks of n neurons.
@@ -70,6 +76,7 @@ struct GrowthDev {
     int* newpost;           // [B][n * 16] new post events of the interval, in order
     int* newpost_cnt;       // [B]
     int* error;
+    int epi_blocks;         // blocks of the bulk-copy epilogue (0: the warp epilogue)
 };
 
 __device__ __forceinline__ size_t gidx(const GrowthDev& g, int b, int i, int j)
@@ -77,13 +84,12 @@ __device__ __forceinline__ size_t gidx(const GrowthDev& g, int b, int i, int j)
     return ((size_t)b * g.n + i) * g.n + j;
 }
 
-// update_synapse, NetworkGrowthSimulator.cpp:16546-16592
-static __device__ __noinline__ void g_update_synapse(const GrowthDev& g, int b, int i, int j)
+// update_synapse, NetworkGrowthSimulator.cpp:16546-16592, for the pair's weight w
+static __device__ __noinline__ void g_update_synapse_w(const GrowthDev& g, int b, int i, int j, double w)
 {
     const SynParams& sp = g.sp;
     const size_t ij = gidx(g, b, i, j);
     const size_t r = (size_t)b * g.n + i;
-    const double w = g.W[ij];
     if ((w >= sp.ACTIVATION_THRESHOLD) && (g.active[ij] == 0) && (g.remodeled[r] == 0)) {
         g.active[ij] = 1;
         g.act_list[r * g.n + g.act_cnt[r]++] = j;
@@ -115,6 +121,11 @@ static __device__ __noinline__ void g_update_synapse(const GrowthDev& g, int b, 
                 break;
             }
     }
+}
+
+static __device__ __forceinline__ void g_update_synapse(const GrowthDev& g, int b, int i, int j)
+{
+    g_update_synapse_w(g, b, i, j, g.W[gidx(g, b, i, j)]);
 }
 
 // LTP / LTD, NetworkGrowthSimulator.cpp:16615-16652
@@ -1026,6 +1037,33 @@ __global__ void __launch_bounds__(kBlock) k_growth_ltp(GrowthDev g, NetDev<R> n,
 // active / super flag, so that test (without the row-state conditions, which only
 // restrict) finds every pair it acts on; lane 0 then runs it on those, in target order.
 // A row's decay and updates read no other row, so rows need no barrier between them.
+// potentiation_decay of one weight (:16346-16361): w -= (w >= SUPERSYNAPSE_THRESHOLD ?
+// BETA_SUPERSYNAPSE : BETA), floor 0; *change: whether update_synapse can act on the pair,
+// i.e. the decayed weight lies on the other side of a threshold than the pair's active
+// or super flag.  With int_thresholds the comparisons are integer comparisons of bit
+// patterns and give the same answers: for weights >= +0 the orders agree; -0 and
+// negative weights (negative as integers) are below positive thresholds in both; and
+// "x < 0" is "sign bit set, and not -0".
+__device__ __forceinline__ double epi_decay(double x, const SynParams& sp, bool act, bool sup, bool* change)
+{
+    if (sp.int_thresholds) {
+        const long long xb = __double_as_longlong(x);
+        x = __dsub_rn(x, xb >= sp.sup_bits ? sp.BETA_SUPERSYNAPSE : sp.BETA);
+        long long yb = __double_as_longlong(x);
+        if (yb < 0 && yb != (long long)0x8000000000000000ull) {
+            x = 0.0;
+            yb = 0;
+        }
+        *change = (yb >= sp.act_bits) != act || (yb >= sp.sup_bits) != sup;
+        return x;
+    }
+    if (x >= sp.SUPERSYNAPSE_THRESHOLD) x -= sp.BETA_SUPERSYNAPSE;
+    else x -= sp.BETA;
+    if (x < 0) x = 0;
+    *change = (x >= sp.ACTIVATION_THRESHOLD) != act || (x >= sp.SUPERSYNAPSE_THRESHOLD) != sup;
+    return x;
+}
+
 __device__ __forceinline__ void g_epilogue_rows(const GrowthDev& g, int b, int row0, int nrows)
 {
     const int lane = threadIdx.x & 31;
@@ -1054,15 +1092,7 @@ __device__ __forceinline__ void g_epilogue_rows(const GrowthDev& g, int b, int r
             for (int k = 0; k < 4; ++k) {
                 const int j = j0 + 32 * k + lane;
                 bool change = false;
-                if (j < g.n) {
-                    double x = w[k];
-                    if (x >= sp.SUPERSYNAPSE_THRESHOLD) x -= sp.BETA_SUPERSYNAPSE;
-                    else x -= sp.BETA;
-                    if (x < 0) x = 0;
-                    Wr[j] = x;
-                    change = (x >= sp.ACTIVATION_THRESHOLD) != (a[k] != 0) ||
-                             (x >= sp.SUPERSYNAPSE_THRESHOLD) != (su[k] != 0);
-                }
+                if (j < g.n) Wr[j] = epi_decay(w[k], sp, a[k] != 0, su[k] != 0, &change);
                 m[k] = __ballot_sync(0xffffffffu, change);
             }
             __syncwarp();   // the decayed weights are visible to lane 0
@@ -1084,6 +1114,103 @@ __global__ void __launch_bounds__(kBlock) k_growth_epilogue(GrowthDev g)
 {
     const int rows = kBlock / 32;   // one row per warp
     g_epilogue_rows(g, (int)blockIdx.y, (int)blockIdx.x * rows, rows);
+}
+
+// The epilogue with the rows staged in shared memory by the bulk copy engine, for
+// networks whose rows start on 16-byte boundaries in every array (n a multiple of 16).
+// A warp owns a row at a time and walks it in chunks of kEpiChunk pairs: lane 0 has the
+// copy engine bring the next chunk's weights and active / super flags into the warp's
+// other buffer while the warp decays the current one in shared memory, runs
+// update_synapse on the pairs that can change (lane 0, in target order), and has the
+// engine write the decayed weights back.  Every wait is bounded; one that gives up sets
+// kErrTimeout and the block stops.
+constexpr int kEpiWarps = 8;
+constexpr int kEpiChunk = 512;
+
+struct EpiBuf {
+    double w[kEpiChunk];
+    uint8_t act[kEpiChunk];
+    uint8_t sup[kEpiChunk];
+};
+
+constexpr size_t kEpiSmem = sizeof(EpiBuf) * 2 * kEpiWarps + sizeof(uint64_t) * 2 * kEpiWarps;
+
+template <class R>
+__global__ void __launch_bounds__(kEpiWarps * 32) k_growth_epilogue_bulk(GrowthDev g)
+{
+    extern __shared__ __align__(128) unsigned char epi_smem[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    EpiBuf* buf = reinterpret_cast<EpiBuf*>(epi_smem) + 2 * warp;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(epi_smem + sizeof(EpiBuf) * 2 * kEpiWarps) + 2 * warp;
+    const SynParams& sp = g.sp;
+    const int n = g.n;
+    const int nch = (n + kEpiChunk - 1) / kEpiChunk;
+    const long long rows = (long long)g.B * n;
+    const long long first_row = (long long)blockIdx.x * kEpiWarps + warp;
+    const long long row_step = (long long)gridDim.x * kEpiWarps;
+    const long long items = first_row < rows ? ((rows - 1 - first_row) / row_step + 1) * nch : 0;
+    if (lane == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    // item t: row first_row + (t / nch) * row_step, chunk t % nch, buffer t & 1
+    auto issue = [&](long long t) {
+        const long long row = first_row + (t / nch) * row_step;
+        const int j0 = (int)(t % nch) * kEpiChunk;
+        const int cnt = min(kEpiChunk, n - j0);
+        const size_t off = (size_t)row * n + j0;
+        EpiBuf& B = buf[t & 1];
+        mbar_arrive_expect_tx(&bar[t & 1], (uint32_t)(cnt * 10));
+        bulk_load(B.w, g.W + off, (uint32_t)(cnt * 8), &bar[t & 1]);
+        bulk_load(B.act, g.active + off, (uint32_t)cnt, &bar[t & 1]);
+        bulk_load(B.sup, g.super + off, (uint32_t)cnt, &bar[t & 1]);
+    };
+    bool ok = true;
+    long long t_fail = 0;
+    if (lane == 0 && items > 0) issue(0);
+    for (long long t = 0; t < items && ok; ++t) {
+        if (lane == 0 && t + 1 < items) {
+            bulk_wait_read<0>();   // the store of item t - 1 has left buffer (t + 1) & 1
+            issue(t + 1);
+        }
+        if (!mbar_wait_bounded(&bar[t & 1], (uint32_t)((t >> 1) & 1))) {
+            ok = false;
+            t_fail = t;
+            break;
+        }
+        const long long row = first_row + (t / nch) * row_step;
+        const int b = (int)(row / n), i = (int)(row % n);
+        const int j0 = (int)(t % nch) * kEpiChunk;
+        const int cnt = min(kEpiChunk, n - j0);
+        EpiBuf& B = buf[t & 1];
+        for (int k = 0; k < kEpiChunk / 32; ++k) {
+            const int c = 32 * k + lane;
+            bool change = false;
+            if (c < cnt) B.w[c] = epi_decay(B.w[c], sp, B.act[c] != 0, B.sup[c] != 0, &change);
+            unsigned m = __ballot_sync(0xffffffffu, change);
+            if (lane == 0)
+                while (m) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1;
+                    g_update_synapse_w(g, b, i, j0 + 32 * k + bit, B.w[32 * k + bit]);
+                }
+        }
+        fence_proxy_async_smem();   // the decayed weights, written by every lane, to the copy engine
+        __syncwarp();
+        if (lane == 0) {
+            bulk_store(g.W + (size_t)row * n + j0, B.w, (uint32_t)(cnt * 8));
+            bulk_commit();
+        }
+    }
+    if (!ok && lane == 0) {
+        atomicOr(g.error, kErrTimeout);
+        // the next item's load may still be in flight into the other buffer: wait for it
+        // (bounded) before the block's shared memory goes away
+        if (t_fail + 1 < items) (void)mbar_wait_bounded(&bar[(t_fail + 1) & 1], (uint32_t)(((t_fail + 1) >> 1) & 1));
+    }
+    if (lane == 0) bulk_wait_all();
 }
 
 // Start of a growth trial: no streams, no pre or post events

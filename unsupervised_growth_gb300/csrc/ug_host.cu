@@ -178,6 +178,13 @@ public:
     // Brings the host copy of the per-trial bookkeeping (activity history, maturation
     // state) up to date with the device, where growth trials keep it.
     virtual ug_status sync_host(cudaStream_t st) = 0;
+    // Per-neuron traces of instance 0 (set_recording): the neurons to record, and the
+    // records of the last trial, [num_steps - 1][4 (RA) | 3 (I)] for the k-th recorded one.
+    virtual ug_status set_recording(const int32_t* ra, int n_ra_rec, const int32_t* in, int n_i_rec,
+                                    cudaStream_t st) = 0;
+    virtual ug_status trace(int which, int k, double* out, cudaStream_t st) = 0;
+    std::vector<int> trace_ra_ids, trace_i_ids;
+    bool traced = false;   // a trial has run since the recording was set
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -257,6 +264,8 @@ public:
     ug_status set_inhibition_tracking(double resolution, cudaStream_t st) override;
     ug_status inhibition(double* out, int32_t* points, double* resolution, cudaStream_t st) override;
     ug_status sync_host(cudaStream_t st) override { return pull_bookkeeping(st); }
+    ug_status set_recording(const int32_t* ra, int n_ra_rec, const int32_t* in, int n_i_rec, cudaStream_t st) override;
+    ug_status trace(int which, int k, double* out, cudaStream_t st) override;
     bool f32_view(ug::NetDev<float>* out) const override
     {
         if constexpr (sizeof(R) == 4) {
@@ -312,6 +321,16 @@ private:
     DevMem gHist_, gHead_, gHsum_, gHact_, gFrl_, gScale_, gMatf_, gRest_, gGca_, gMature_, gTar_, gRepCnt_, gLoop_;
     ug::TailDev<R> td_{};
     bool book_dirty_ = false;      // the device bookkeeping changed since the host copy was read
+    DevMem gTrRaSlot_, gTrISlot_, gTrRaBuf_, gTrIBuf_;   // per-neuron traces
+    void apply_recording()
+    {
+        const bool on = !trace_ra_ids.empty() || !trace_i_ids.empty();
+        bd_.trace_ra = on && !trace_ra_ids.empty() ? gTrRaSlot_.as<int>() : nullptr;
+        bd_.trace_i = on && !trace_i_ids.empty() ? gTrISlot_.as<int>() : nullptr;
+        bd_.trace_ra_buf = gTrRaBuf_.as<double>();
+        bd_.trace_i_buf = gTrIBuf_.as<double>();
+        if (on) traced = true;
+    }
     int* hloop_ = nullptr;         // pinned copy of the loop words
     cudaGraphExec_t gloop_ = nullptr;   // the multi-trial loop: a WHILE node around one growth trial
     int gloop_training_ = -1;
@@ -716,6 +735,7 @@ ug_status NetImpl<R>::prepare_test(uint32_t first_trial, int n_trials, cudaStrea
     bd_.B = n_trials;
     bd_.kick_on = 1;
     bd_.scatter_rara = 1;
+    apply_recording();
     // capacity errors belong to the batch that raised them
     UG_CUDA(cudaMemsetAsync(error_.as<int>(), 0, sizeof(int), st));
     B_ = n_trials;
@@ -734,6 +754,7 @@ ug_status NetImpl<R>::check_error(cudaStream_t st)
     UG_CUDA(cudaStreamSynchronize(st));
     int err = 0;
     UG_CUDA(cudaMemcpy(&err, error_.as<int>(), sizeof(int), cudaMemcpyDeviceToHost));
+    if (err & ug::kErrTimeout) return fail(UG_ETIMEOUT, "a bounded device wait gave up");
     if (err & ug::kErrSpikeCapacity) return fail(UG_ECAPACITY, "spike record buffer overflowed; raise spike_capacity_per_neuron");
     if (err) return fail(UG_ECAPACITY, "device event buffer overflowed");
     return UG_OK;
@@ -873,6 +894,12 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     g.sp.TAU_P = h.syn.TAU_P; g.sp.TAU_D = h.syn.TAU_D; g.sp.BETA = h.syn.BETA;
     g.sp.BETA_SUPERSYNAPSE = h.syn.BETA_SUPERSYNAPSE; g.sp.ACTIVATION_THRESHOLD = h.syn.ACTIVATION_THRESHOLD;
     g.sp.SUPERSYNAPSE_THRESHOLD = h.syn.SUPERSYNAPSE_THRESHOLD; g.sp.WEIGHT_MAX = h.syn.WEIGHT_MAX;
+    g.sp.int_thresholds = (h.syn.ACTIVATION_THRESHOLD > 0.0 && h.syn.SUPERSYNAPSE_THRESHOLD > 0.0 &&
+                           std::isfinite(h.syn.ACTIVATION_THRESHOLD) && std::isfinite(h.syn.SUPERSYNAPSE_THRESHOLD))
+                              ? 1 : 0;
+    std::memcpy(&g.sp.act_bits, &h.syn.ACTIVATION_THRESHOLD, sizeof(double));
+    std::memcpy(&g.sp.sup_bits, &h.syn.SUPERSYNAPSE_THRESHOLD, sizeof(double));
+    UG_CUDA(ug::epilogue_bulk_grid<R>(n, 1, &g.epi_blocks));
     g.W = gW_.as<double>(); g.D = gD_.as<double>(); g.perm = gPerm_.as<int>();
     g.active = gActive_.as<uint8_t>(); g.super = gSuper_.as<uint8_t>();
     g.act_list = gActList_.as<int>(); g.act_cnt = gActCnt_.as<int>();
@@ -1146,6 +1173,7 @@ ug_status NetImpl<R>::prepare_growth_run(int training, cudaStream_t st)
     td_.nsoma = ra_nsoma_.as<int>();
     td_.trial_dev = trial_.as<uint32_t>();
     td_.mean_inj = mean_inj_.as<double>();
+    apply_recording();
     return UG_OK;
 }
 
@@ -1266,6 +1294,8 @@ ug_status NetImpl<R>::member(ug::GroupMember<R>* m, int index, int2* act_rows, i
     m->rc = rc_;
     m->ic = ic_;
     m->bt.member = index;
+    m->bt.trace_ra = nullptr;   // traces are recorded by single-network runs only
+    m->bt.trace_i = nullptr;
     m->bt.act_rows = nullptr;
     m->bt.act_cnt = nullptr;
     m->bt.live_streams = nullptr;
@@ -1424,6 +1454,60 @@ ug_status NetImpl<R>::replace_neurons(const std::vector<int>& rep, uint32_t tria
     UG_CUDA(cudaStreamSynchronize(st));
     UG_TRY(upload_connectivity(st));
     UG_CUDA(cudaStreamSynchronize(st));
+    return UG_OK;
+}
+
+// set_recording (NetworkGrowthSimulator.cpp:2352-2407): the neurons whose state is
+// recorded before every step of instance 0 of the next trials.
+template <class R>
+ug_status NetImpl<R>::set_recording(const int32_t* ra, int n_ra_rec, const int32_t* in, int n_i_rec, cudaStream_t st)
+{
+    if (n_ra_rec < 0 || n_i_rec < 0 || n_ra_rec > 1024 || n_i_rec > 1024)
+        return fail(UG_EINVAL, "at most 1024 recorded neurons of each kind");
+    if ((n_ra_rec && !ra) || (n_i_rec && !in)) return fail(UG_EINVAL, "null neuron list");
+    std::vector<int> slot_ra(h.n_ra, -1), slot_i(std::max(h.n_i, 1), -1);
+    std::vector<int> ids_ra, ids_i;
+    for (int k = 0; k < n_ra_rec; ++k) {
+        if (ra[k] < 0 || ra[k] >= h.n_ra) return fail(UG_EINVAL, "recorded HVC(RA) id out of range");
+        if (slot_ra[ra[k]] >= 0) return fail(UG_EINVAL, "a HVC(RA) neuron is listed twice");
+        slot_ra[ra[k]] = k;
+        ids_ra.push_back(ra[k]);
+    }
+    for (int k = 0; k < n_i_rec; ++k) {
+        if (in[k] < 0 || in[k] >= h.n_i) return fail(UG_EINVAL, "recorded HVC(I) id out of range");
+        if (slot_i[in[k]] >= 0) return fail(UG_EINVAL, "a HVC(I) neuron is listed twice");
+        slot_i[in[k]] = k;
+        ids_i.push_back(in[k]);
+    }
+    trace_ra_ids.clear();
+    trace_i_ids.clear();
+    traced = false;
+    drop_graphs();   // the recording variants of the integrators and the buffers change
+    UG_TRY(gTrRaSlot_.upload(slot_ra, st));
+    UG_TRY(gTrISlot_.upload(slot_i, st));
+    const size_t steps = (size_t)h.num_steps;
+    UG_TRY(gTrRaBuf_.alloc(std::max<size_t>(ids_ra.size(), 1) * steps * 4 * sizeof(double)));
+    UG_TRY(gTrIBuf_.alloc(std::max<size_t>(ids_i.size(), 1) * steps * 3 * sizeof(double)));
+    UG_CUDA(cudaStreamSynchronize(st));
+    trace_ra_ids = ids_ra;
+    trace_i_ids = ids_i;
+    return UG_OK;
+}
+
+template <class R>
+ug_status NetImpl<R>::trace(int which, int k, double* out, cudaStream_t st)
+{
+    const std::vector<int>& ids = which == 0 ? trace_ra_ids : trace_i_ids;
+    if (which != 0 && which != 1) return fail(UG_EINVAL, "which: 0 HVC(RA), 1 HVC(I)");
+    if (k < 0 || k >= (int)ids.size()) return fail(UG_EINVAL, "no such recorded neuron");
+    if (!traced) return fail(UG_EINVAL, "no trial has run since the recording was set");
+    UG_TRY(check_error(st));
+    const int w = which == 0 ? 4 : 3;
+    const size_t steps = (size_t)h.num_steps;
+    const DevMem& buf = which == 0 ? gTrRaBuf_ : gTrIBuf_;
+    // rows for steps 1 .. num_steps - 1 (row st - 1 holds the state before step st)
+    UG_CUDA(cudaMemcpy(out, buf.as<double>() + ((size_t)k * steps + 1) * w, (steps - 1) * w * sizeof(double),
+                       cudaMemcpyDeviceToHost));
     return UG_OK;
 }
 
@@ -2378,6 +2462,50 @@ ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out)
     for (int i = 0; i < n->h.n_ra; ++i)
         for (int k = 0; k < W; ++k)
             out[(size_t)i * W + k] = n->h.hist[(size_t)i * W + (n->h.hist_head + k) % W];
+    return UG_OK;
+}
+
+ug_status ug_set_recording(ug_ctx* ctx, int32_t net_id, const int32_t* ra_ids, int32_t n_ra_ids, const int32_t* i_ids,
+                           int32_t n_i_ids)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    return n->set_recording(ra_ids, n_ra_ids, i_ids, n_i_ids, ctx->stream);
+}
+
+ug_status ug_get_trace(ug_ctx* ctx, int32_t net_id, int32_t which, int32_t k, double* out, int32_t* n_records)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    const int records = n->h.num_steps - 1;
+    if (n_records) *n_records = records;
+    if (!out) return UG_OK;
+    const int w = which == 0 ? 4 : 3;
+    std::vector<double> v((size_t)records * w);
+    UG_TRY(n->trace(which, k, v.data(), ctx->stream));
+    // (time before the step, state...), the record of HH2_test / HHI_buffer::record_state
+    for (int r = 0; r < records; ++r) {
+        out[(size_t)r * (w + 1)] = n->T[r];
+        for (int c = 0; c < w; ++c) out[(size_t)r * (w + 1) + 1 + c] = v[(size_t)r * w + c];
+    }
+    return UG_OK;
+}
+
+ug_status ug_get_recording(ug_ctx* ctx, int32_t net_id, int32_t* ra_ids, int32_t* n_ra_ids, int32_t* i_ids,
+                           int32_t* n_i_ids)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (n_ra_ids) *n_ra_ids = (int32_t)n->trace_ra_ids.size();
+    if (n_i_ids) *n_i_ids = (int32_t)n->trace_i_ids.size();
+    if (ra_ids) std::copy(n->trace_ra_ids.begin(), n->trace_ra_ids.end(), ra_ids);
+    if (i_ids) std::copy(n->trace_i_ids.begin(), n->trace_i_ids.end(), i_ids);
     return UG_OK;
 }
 

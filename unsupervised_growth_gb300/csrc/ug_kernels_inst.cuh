@@ -31,7 +31,11 @@ inline void launch_i(const NetDev<double>& n, const BatchDev<double>& b, int q, 
                      const IStep<double>& ic, cudaStream_t st, const LaunchCtx& lc)
 {
     if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
-    k_interval_i<double><<<dim3((n.n_i + kBlock - 1) / kBlock, b.B), kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    const dim3 g((n.n_i + kBlock - 1) / kBlock, b.B);
+    if (b.trace_i)
+        k_interval_i<double, true><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    else
+        k_interval_i<double><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
     if (lc.timer) lc.timer->end(lc.main);
 }
 
@@ -39,7 +43,11 @@ inline void launch_i(const NetDev<float>& n, const BatchDev<float>& b, int q, in
                      cudaStream_t st, const LaunchCtx& lc)
 {
     if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
-    k_interval_i_x<float><<<dim3((n.n_i + kBlock - 1) / kBlock, b.B), kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    const dim3 g((n.n_i + kBlock - 1) / kBlock, b.B);
+    if (b.trace_i)
+        k_interval_i_x<float, true><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+    else
+        k_interval_i_x<float><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
     if (lc.timer) lc.timer->end(lc.main);
 }
 
@@ -59,7 +67,7 @@ inline void launch_ra(const NetDev<double>& n, const BatchDev<double>& b, int q,
 {
     const dim3 g((n.n_ra + kBlock - 1) / kBlock, b.B);
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
-    if (b.ginh_slot)
+    if (b.ginh_slot || b.trace_ra)
         k_interval_ra<double, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
     else
         k_interval_ra<double><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
@@ -71,7 +79,7 @@ inline void launch_ra(const NetDev<float>& n, const BatchDev<float>& b, int q, i
 {
     const dim3 g(((n.n_ra + 1) / 2 + kBlock - 1) / kBlock, b.B);
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
-    if (b.ginh_slot)
+    if (b.ginh_slot || b.trace_ra)
         k_interval_ra_x2<float, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
     else
         k_interval_ra_x2<float><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
@@ -147,9 +155,35 @@ cudaError_t launch_growth_sync(const GrowthDev& g, const NetDev<R>& n, const Bat
 template <class R>
 cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc)
 {
+    if (g.epi_blocks > 0) {   // rows staged by the bulk copy engine
+        UG_TIMED(lc, "k_growth_epilogue", (k_growth_epilogue_bulk<R><<<g.epi_blocks, kEpiWarps * 32, kEpiSmem, lc.main>>>(g)));
+        return cudaGetLastError();
+    }
     const dim3 rows((g.n + kBlock / 32 - 1) / (kBlock / 32), g.B);   // a warp per row
     UG_TIMED(lc, "k_growth_epilogue", (k_growth_epilogue<R><<<rows, kBlock, 0, lc.main>>>(g)));
     return cudaGetLastError();
+}
+
+// Grid of the bulk-copy epilogue for B networks of n neurons (0: rows not 16-byte aligned
+// in every array, so the warp epilogue runs), after allowing its shared memory.
+template <class R>
+cudaError_t epilogue_bulk_grid(int n, int B, int* blocks)
+{
+    *blocks = 0;
+    if (n % 16 != 0 || n <= 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(k_growth_epilogue_bulk<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kEpiSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_growth_epilogue_bulk<R>, kEpiWarps * 32, kEpiSmem);
+    if (e != cudaSuccess) return e;
+    const long long rows = (long long)n * B;
+    const long long want = (rows + kEpiWarps - 1) / kEpiWarps;
+    *blocks = (int)std::min<long long>(want, (long long)std::max(per_sm, 1) * sms);
+    return cudaSuccess;
 }
 
 template <class R>

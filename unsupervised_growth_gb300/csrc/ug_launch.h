@@ -126,6 +126,8 @@ cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc);
 template <class R>
 cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st);
 template <class R>
+cudaError_t epilogue_bulk_grid(int n, int B, int* blocks);
+template <class R>
 cudaError_t launch_check_bad(const NetDev<R>& n, const BatchDev<R>& b, int* bad, cudaStream_t st);
 // The device tail of a growth trial and the head of the next (ug_tail.cuh).
 template <class R>

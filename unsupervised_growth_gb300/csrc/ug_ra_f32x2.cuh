@@ -7,6 +7,7 @@
 //  * exponentials are MUFU ex2 with log2(e) folded into the affine argument;
 //  * the seven reciprocals of a stage (mInf, nInf/tauN, lInf, hInf/tauH, rInf,
 //    cInf and ca/(ca+6)) come from two MUFU rcp: 1/a = b/(ab) etc.
+//  * (x - c) k products are single multiply-adds with the constants folded in.
 // Per neuron and step: 32 ex2 + 8 rcp on the SFU.
 #pragma once
 #include "ug_neuron.cuh"
@@ -45,7 +46,22 @@ struct RA2 { f2 Vs, Vd, n, h, l, r, c, Ca; };
 struct RAPair {
     f2 EL, GdCa;       // per-neuron parameters
     f2 mus, mud;       // 100000 mu / A
+    f2 cs, cd;         // GsL EL + mus and GdL EL + mud: the constant parts of the leak terms
 };
+
+// The per-neuron constants of a pair.
+__device__ __forceinline__ RAPair ra_pair(f2 EL, f2 GdCa, float mus, float mud)
+{
+    typedef RAConst K;
+    RAPair P;
+    P.EL = EL;
+    P.GdCa = GdCa;
+    P.mus = S(mus);
+    P.mud = S(mud);
+    P.cs = fma2(EL, S((float)K::GsL), S(mus));
+    P.cd = fma2(EL, S((float)K::GdL), S(mud));
+    return P;
+}
 
 __device__ __forceinline__ RA2 ra_rhs_x2(const RA2& y, f2 Ge, f2 Gi, const RAPair& P)
 {
@@ -87,19 +103,20 @@ __device__ __forceinline__ RA2 ra_rhs_x2(const RA2& y, f2 Ge, f2 Gi, const RAPai
     const f2 m3 = m * m * m;
     const f2 n2 = y.n * y.n;
     const f2 n4 = n2 * n2;
-    // kVs
-    f2 t = (vs - P.EL) * S(-(float)K::GsL);
-    t = fma2(m3 * y.h, (vs - S((float)K::EsNa)) * S(-(float)K::GsNa), t);
-    t = fma2(fma2(n4, S((float)K::GsK), y.l * S((float)K::GsKLT)), (vs - S((float)K::EsK)) * S(-1.0f), t);
-    t = t + P.mus;
+    // kVs = GsL (EL - vs) + GsNa m^3 h (EsNa - vs) + (GsK n^4 + GsKLT l)(EsK - vs) + mus
+    //       + (vd - vs) 100000 / (Rc As); every (x - c) k is one multiply-add
+    f2 t = fma2(vs, S(-(float)K::GsL), P.cs);
+    t = fma2(m3 * y.h, fma2(vs, S(-(float)K::GsNa), S((float)(K::GsNa * K::EsNa))), t);
+    t = fma2(fma2(n4, S((float)K::GsK), y.l * S((float)K::GsKLT)), S((float)K::EsK) - vs, t);
     k.Vs = fma2(vd - vs, S((float)(100000.0 / (K::Rc * K::As))), t);
-    // kVd: GdCaK (vd - EdK) c ca / (ca + 6)
-    f2 u = (vd - P.EL) * S(-(float)K::GdL);
-    u = fma2(P.GdCa * y.r * y.r, (vd - S((float)K::EdCa)) * S(-1.0f), u);
+    // kVd = GdL (EL - vd) + GdCa r^2 (EdCa - vd) - GdCaK (vd - EdK) c ca / (ca + 6)
+    //       - Ge vd + Gi (Egaba - vd) + mud + (vs - vd) 100000 / (Rc Ad)
+    const f2 gr2 = P.GdCa * y.r * y.r;
+    const f2 eca = S((float)K::EdCa) - vd;
+    f2 u = fma2(vd, S(-(float)K::GdL), P.cd);
+    u = fma2(gr2, eca, u);
     u = fma2((vd - S((float)K::EdK)) * y.c, y.Ca * iDca * S(-(float)K::GdCaK), u);
-    u = fma2(Ge, vd * S(-1.0f), u);
-    u = fma2(Gi, (vd - S((float)K::Egaba)) * S(-1.0f), u);
-    u = u + P.mud;
+    u = fma2(Ge + Gi, S(0.0f) - vd, fma2(Gi, S((float)K::Egaba), u));
     k.Vd = fma2(vs - vd, S((float)(100000.0 / (K::Rc * K::Ad))), u);
     // kn = (nInf - n)/tauN = (1 - n an) bn / Dn ; kh likewise
     k.n = fma2(y.n * S(-1.0f), an, S(1.0f)) * bn * iDn;
@@ -107,7 +124,7 @@ __device__ __forceinline__ RA2 ra_rhs_x2(const RA2& y, f2 Ge, f2 Gi, const RAPai
     k.l = (iDl - y.l) * S(0.1f);
     k.r = iDr - y.r;
     k.c = (iDc - y.c) * S(1.0f / 15.0f);
-    k.Ca = fma2(P.GdCa * y.r * y.r, (vd - S((float)K::EdCa)) * S(-0.1f), y.Ca * S(-0.02f));
+    k.Ca = fma2(gr2, eca * S(0.1f), y.Ca * S(-0.02f));
     return k;
 }
 
@@ -123,17 +140,19 @@ __device__ __forceinline__ void ra_debrabant_x2(RA2& s, f2& Ge, f2& Gi, const RA
     const f2 nd = S(p.sq * p.sig_d * (float)(1.0 / (K::Ad * K::cm)));
     const f2 Ge1 = Ge * S(p.e1), Gi1 = Gi * S(p.e1), Ge2 = Ge * S(p.e2), Gi2 = Gi * S(p.e2);
 
+    // the noise amplitudes times the step's point values, once per step
+    const f2 a1s = ns * J1s, a2s = ns * J2s, a1d = nd * J1d, a2d = nd * J2d;
     RA2 y = s;
-    y.Vs = fma2(ns, fma2(J1s, S(-0.01844540496323970f), J2s * S(-0.1866426386543421f)), s.Vs);
-    y.Vd = fma2(nd, fma2(J1d, S(-0.01844540496323970f), J2d * S(-0.1866426386543421f)), s.Vd);
+    y.Vs = fma2(a1s, S(-0.01844540496323970f), fma2(a2s, S(-0.1866426386543421f), s.Vs));
+    y.Vd = fma2(a1d, S(-0.01844540496323970f), fma2(a2d, S(-0.1866426386543421f), s.Vd));
     const RA2 a1 = ra_rhs_x2(y, Ge, Gi, P);
 
     RA2 h4, up;   // running sums of stage 4's increment and of the update
 #define M(f) h4.f = a1.f * S(-0.4526683126055039f); up.f = a1.f * S(1.0f / 6.0f); y.f = fma2(dt, a1.f, s.f);
     UG_RA2_FOR(M)
 #undef M
-    y.Vs = fma2(ns, fma2(J1s, S(0.8017012756521233f), J2s * S(-0.8575745885712401f)), y.Vs);
-    y.Vd = fma2(nd, fma2(J1d, S(0.8017012756521233f), J2d * S(-0.8575745885712401f)), y.Vd);
+    y.Vs = fma2(a1s, S(0.8017012756521233f), fma2(a2s, S(-0.8575745885712401f), y.Vs));
+    y.Vd = fma2(a1d, S(0.8017012756521233f), fma2(a2d, S(-0.8575745885712401f), y.Vd));
     const RA2 a2 = ra_rhs_x2(y, Ge1, Gi1, P);
 
     const f2 d8 = S(p.dt * 0.125f);
@@ -141,23 +160,23 @@ __device__ __forceinline__ void ra_debrabant_x2(RA2& s, f2& Ge, f2& Gi, const RA
              y.f = fma2(d8, fma2(a1.f, S(3.0f), a2.f), s.f);
     UG_RA2_FOR(M)
 #undef M
-    y.Vs = fma2(ns, fma2(J1s, S(0.5092227024816198f), J2s * S(-0.4723392695015512f)), y.Vs);
-    y.Vd = fma2(nd, fma2(J1d, S(0.5092227024816198f), J2d * S(-0.4723392695015512f)), y.Vd);
+    y.Vs = fma2(a1s, S(0.5092227024816198f), fma2(a2s, S(-0.4723392695015512f), y.Vs));
+    y.Vd = fma2(a1d, S(0.5092227024816198f), fma2(a2d, S(-0.4723392695015512f), y.Vd));
     const RA2 a3 = ra_rhs_x2(y, Ge2, Gi2, P);
 
 #define M(f) h4.f = fma2(a3.f, S(1.9368910834740051f), h4.f); up.f = fma2(a3.f, S(2.0f / 3.0f), up.f); \
              y.f = fma2(dt, h4.f, s.f);
     UG_RA2_FOR(M)
 #undef M
-    y.Vs = fma2(ns, fma2(J1s, S(0.9758794209767762f), J2s * S(0.3060354860326548f)), y.Vs);
-    y.Vd = fma2(nd, fma2(J1d, S(0.9758794209767762f), J2d * S(0.3060354860326548f)), y.Vd);
+    y.Vs = fma2(a1s, S(0.9758794209767762f), fma2(a2s, S(0.3060354860326548f), y.Vs));
+    y.Vd = fma2(a1d, S(0.9758794209767762f), fma2(a2d, S(0.3060354860326548f), y.Vd));
     const RA2 a4 = ra_rhs_x2(y, Ge1, Gi1, P);
 
 #define M(f) s.f = fma2(dt, fma2(a4.f, S(0.1720970973419255f), up.f), s.f);
     UG_RA2_FOR(M)
 #undef M
-    s.Vs = fma2(ns * S(100000.0f), J1s, s.Vs);
-    s.Vd = fma2(nd * S(100000.0f), J1d, s.Vd);
+    s.Vs = fma2(a1s, S(100000.0f), s.Vs);
+    s.Vd = fma2(a1d, S(100000.0f), s.Vd);
     Ge = Ge1;
     Gi = Gi1;
 }

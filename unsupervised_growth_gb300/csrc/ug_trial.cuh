@@ -38,7 +38,7 @@ constexpr int kBlock = 128;
 #endif
 
 enum SpikeKind { kSpikeSoma = 0, kSpikeDend = 1, kSpikeInter = 2 };
-enum DevError { kErrSpikeCapacity = 1, kErrEventCapacity = 2, kErrPostCapacity = 4 };
+enum DevError { kErrSpikeCapacity = 1, kErrEventCapacity = 2, kErrPostCapacity = 4, kErrTimeout = 8 };
 
 template <class R>
 struct NetDev {
@@ -98,7 +98,37 @@ struct BatchDev {
     // (slot 0) and after each step st with ginh_slot[st] > 0, in that slot.
     R* ginh_rec;               // [points][B][n_ra], or null
     const int* ginh_slot;      // [num_steps] slot recorded after step st, or -1
+    // Per-neuron traces of instance 0 (set_recording, NetworkGrowthSimulator.cpp:2352-2407):
+    // the state before each step st, as HH2_test::record_state / HHI_buffer::record_state
+    // keep it (HH2_test.cpp:476-497, HHI_buffer.cpp:148-167).
+    const int* trace_ra;       // [n_ra] slot of each recorded HVC(RA) neuron, -1 if not recorded; or null
+    const int* trace_i;        // [n_i] likewise for HVC(I)
+    double* trace_ra_buf;      // [slots][num_steps][4]: Vs, Vd, Gexc_d, Ginh_d
+    double* trace_i_buf;       // [slots][num_steps][3]: V, Gexc, Ginh
 };
+
+// The state of a recorded neuron before step st of instance 0 (the recording variants only).
+template <class R>
+__device__ __forceinline__ void trace_ra_row(const BatchDev<R>& bt, int num_steps, int b, int i, int st, R vs, R vd,
+                                             R ge, R gi)
+{
+    if (b != 0 || !bt.trace_ra) return;
+    const int sl = bt.trace_ra[i];
+    if (sl < 0) return;
+    double* r = bt.trace_ra_buf + ((size_t)sl * num_steps + st) * 4;
+    r[0] = (double)vs; r[1] = (double)vd; r[2] = (double)ge; r[3] = (double)gi;
+}
+
+template <class R>
+__device__ __forceinline__ void trace_i_row(const BatchDev<R>& bt, int num_steps, int b, int i, int st, R v, R ge,
+                                            R gi)
+{
+    if (b != 0 || !bt.trace_i) return;
+    const int sl = bt.trace_i[i];
+    if (sl < 0) return;
+    double* r = bt.trace_i_buf + ((size_t)sl * num_steps + st) * 3;
+    r[0] = (double)v; r[1] = (double)ge; r[2] = (double)gi;
+}
 
 // Queues row x of a group growth member for interval q if it has deliveries to make.
 template <class R>
@@ -363,6 +393,7 @@ __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const Batch
         RAStep<R> p = rc;
         for (int st = s0; st <= s1; ++st) {
             if (st == kick) s.Ge = s.Ge + R(3.0);   // raiseE(G_TRAINING_KICK)
+            if constexpr (kTrack) trace_ra_row(bt, n.num_steps, b, i, st, s.Vs, s.Vd, s.Ge, s.Gi);
             load_ra_step(n, p, st);
             bool fs, fd;
             ra_step(s, flags, fs, fd, EL, GdCa, p, sid, (uint32_t)st);
@@ -452,17 +483,19 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
                 Ge.y = Ge.y + (float)(((double)ae1 * kFixInv) / RAConst::Ad);
             }
         }
-        RAPair P;
-        P.EL = make_float2(n.Erest[i0], n.Erest[v1 ? i1 : i0]);
-        P.GdCa = make_float2(n.GCa[i0], n.GCa[v1 ? i1 : i0]);
-        P.mus = S((float)(100000.0 / RAConst::As) * rc.mu_s);
-        P.mud = S((float)(100000.0 / RAConst::Ad) * rc.mu_d);
+        const RAPair P = ra_pair(make_float2(n.Erest[i0], n.Erest[v1 ? i1 : i0]),
+                                 make_float2(n.GCa[i0], n.GCa[v1 ? i1 : i0]),
+                                 (float)(100000.0 / RAConst::As) * rc.mu_s, (float)(100000.0 / RAConst::Ad) * rc.mu_d);
         const int k0 = bt.kick_step[x0], k1 = v1 ? bt.kick_step[x1] : 0x7fffffff;
         const StreamId sid0 = make_stream(n.seed, kNoiseRAWhite, n.net_id, (uint32_t)i0, bt.trial[b]);
         const uint32_t ent1 = (uint32_t)(v1 ? i1 : i0);
         for (int st = s0; st <= s1; ++st) {
             if (st == k0) Ge.x = Ge.x + 3.0f;   // raiseE(G_TRAINING_KICK)
             if (st == k1) Ge.y = Ge.y + 3.0f;
+            if constexpr (kTrack) {
+                trace_ra_row(bt, n.num_steps, b, i0, st, s.Vs.x, s.Vd.x, Ge.x, Gi.x);
+                if (v1) trace_ra_row(bt, n.num_steps, b, i1, st, s.Vs.y, s.Vd.y, Ge.y, Gi.y);
+            }
             bool fs, fd;
             RAState<float> c0, c1;
             c0.Vs = s.Vs.x; c0.Vd = s.Vd.x; c1.Vs = s.Vs.y; c1.Vd = s.Vd.y;
@@ -584,7 +617,7 @@ __global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R
 
 // Single-precision HVC(I) part of one interval: noise kicks from the pre-drawn
 // events, DP8 in the layout of ug_i_f32.cuh.
-template <class R>
+template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                   const IStep<R>& ic, int bx, int b)
 {
@@ -611,6 +644,7 @@ __device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const Batc
         int2 ne = eve[ie], ni = evi[ii];
         int flag = bt.i_flag[x];
         for (int st = s0; st <= s1; ++st) {
+            if constexpr (kTrack) trace_i_row(bt, n.num_steps, b, i, st, s.V, s.Ge, s.Gi);
             if (i_state_check(s.V, flag)) fired_bits |= 1u << (st - s0);
             if (st == ne.x) {
                 s.Ge += __int_as_float(ne.y);
@@ -637,15 +671,15 @@ __device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const Batc
                  n.i2ra_d, bt.ring_ra_inh, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
 }
 
-template <class R>
+template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
                                                                          IStep<R> ic)
 {
-    interval_i_x_body(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
+    interval_i_x_body<R, kTrack>(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 // HVC(I) part of one interval; scatters the I->RA kicks of its spikes.
-template <class R>
+template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                 const IStep<R>& ic, int bx, int b)
 {
@@ -672,6 +706,7 @@ __device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchD
         const StreamId sid = make_stream(n.seed, kNoiseIPoisson, n.net_id, (uint32_t)i, bt.trial[b]);
         IStep<R> p = ic;
         for (int st = s0; st <= s1; ++st) {
+            if constexpr (kTrack) trace_i_row(bt, n.num_steps, b, i, st, s.V, s.Ge, s.Gi);
             if (i_state_check(s.V, flag)) fired_bits |= 1u << (st - s0);
             if (st == se) se = i_noise_event(n.T, n.num_steps, st, ne, s.Ge, sid, word);
             if (st == si) si = i_noise_event(n.T, n.num_steps, st, ni, s.Gi, sid, word);
@@ -696,11 +731,11 @@ __device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchD
                  n.i2ra_d, bt.ring_ra_inh, (size_t)bt.B * n.n_ra, (size_t)b * n.n_ra);
 }
 
-template <class R>
+template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_i(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
                                                                               IStep<R> ic)
 {
-    interval_i_body(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
+    interval_i_body<R, kTrack>(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
 }
 
 }  // namespace ug

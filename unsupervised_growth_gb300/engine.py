@@ -35,7 +35,8 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_write_inhibition_tracking_state", "ug_generate_topology", "ug_topology_get_info",
             "ug_topology_get_coordinates", "ug_topology_get_connections", "ug_topology_get_training",
             "ug_topology_write_dir", "ug_topology_free", "ug_create_growth_network_from_topology",
-            "ug_create_network_topology", "ug_calibrate_pipes"]
+            "ug_create_network_topology", "ug_calibrate_pipes", "ug_probe_bounded_wait", "ug_set_recording",
+            "ug_get_recording", "ug_get_trace", "ug_write_traces"]
 
 
 class UGError(RuntimeError):
@@ -195,6 +196,11 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_kernel_timing.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.ug_run_test_trial_noalloc.argtypes = [vp, C.c_int32, C.c_uint32] + [C.c_void_p] * 6
     L.ug_calibrate_pipes.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.ug_probe_bounded_wait.argtypes = [C.c_int32, C.c_int32]
+    L.ug_set_recording.argtypes = [C.c_void_p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32]
+    L.ug_get_recording.argtypes = [C.c_void_p, C.c_int32, _i32p, C.POINTER(C.c_int32), _i32p, C.POINTER(C.c_int32)]
+    L.ug_get_trace.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.POINTER(C.c_int32)]
+    L.ug_write_traces.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int32]
     L.ug_set_inhibition_tracking.argtypes = [vp, C.c_int32, C.c_double]
     L.ug_get_inhibitory_conductance.argtypes = [vp, C.c_int32, _f64p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     L.ug_write_inhibition_tracking_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
@@ -377,6 +383,26 @@ class ResidentNetwork:
         out = np.zeros((self.net.n_ra, n.value))
         _check(L.ug_get_inhibitory_conductance(self.engine.ctx, self.id, _ptr(out, _f64p), C.byref(n), C.byref(res)))
         return out, res.value
+
+    def set_recording(self, ra_ids=(), i_ids=()):
+        """Record the state of these neurons before every step of the next trials
+        (instance 0 of test batches, and growth trials run alone); empty lists: off."""
+        ra = np.ascontiguousarray(ra_ids, dtype=np.int32)
+        ii = np.ascontiguousarray(i_ids, dtype=np.int32)
+        _check(self.engine.L.ug_set_recording(self.engine.ctx, self.id, _ptr(ra, _i32p), len(ra), _ptr(ii, _i32p),
+                                              len(ii)))
+
+    def trace(self, which: int, k: int):
+        """The last trial's trace of the k-th recorded neuron: rows (time, Vs, Vd, Gexc_d, Ginh_d)
+        for HVC(RA) (which 0) or (time, V, Gexc, Ginh) for HVC(I) (which 1), one per step."""
+        L, n = self.engine.L, C.c_int32(0)
+        _check(L.ug_get_trace(self.engine.ctx, self.id, which, k, None, C.byref(n)))
+        out = np.zeros((n.value, 5 if which == 0 else 4))
+        _check(L.ug_get_trace(self.engine.ctx, self.id, which, k, _ptr(out, _f64p), C.byref(n)))
+        return out
+
+    def write_traces(self, directory: str, trial: int):
+        _check(self.engine.L.ug_write_traces(self.engine.ctx, self.id, directory.encode(), trial))
 
     def write_inhibition_tracking_state(self, directory: str, trial: int):
         _check(self.engine.L.ug_write_inhibition_tracking_state(self.engine.ctx, self.id, directory.encode(), trial))
@@ -588,6 +614,13 @@ def calibrate_pipes(device: int = 0):
     a, b = C.c_double(0), C.c_double(0)
     _check(L.ug_calibrate_pipes(device, C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+def probe_bounded_wait(device: int = 0, which: int = 0) -> str:
+    """Runs a device wait that nothing can satisfy (0: a global flag, 1: an mbarrier) and
+    returns the status name it ends with (UG_ETIMEOUT once the bounded wait gives up)."""
+    L = load_library()
+    return UG_STATUS.get(L.ug_probe_bounded_wait(device, which), "unknown")
 
 
 def make_desc(net: Network):
