@@ -473,10 +473,17 @@ FAST_MAT = dict(RATE_WINDOW_LONG=1000, E_REST_IMMATURE=-65.0, GCA_IMMATURE=25.0,
 
 
 def make_growth_network(num_steps=NUM_STEPS, fast=False):
+    """The config-2 network; `fast`: fast-growing synapses, with the ten training neurons
+    spread over 15 ms so that they potentiate onto one another and supersynapses form."""
+    import numpy as np
+
     from unsupervised_growth_gb300.network import synthetic_growth_network
     extra = dict(syn=FAST_SYN, mat=FAST_MAT) if fast else {}
-    return synthetic_growth_network(n_ra=N_RA, n_i=N_I, n_tr=10, seed=2, delays="lognormal", lognormal_mean=3.0,
-                                    lognormal_sigma=1.5, delay_cap=10.0, num_steps=num_steps, **extra)
+    net = synthetic_growth_network(n_ra=N_RA, n_i=N_I, n_tr=10, seed=2, delays="lognormal", lognormal_mean=3.0,
+                                   lognormal_sigma=1.5, delay_cap=10.0, num_steps=num_steps, **extra)
+    if fast:
+        net.training_spread = np.linspace(0.0, 15.0, len(net.training))
+    return net
 
 
 def run_growth(args, local_rank):
@@ -502,6 +509,7 @@ def run_growth(args, local_rank):
         eng.synchronize()
         wall = time.perf_counter() - t0
     launches = eng.launch_count() - l0
+    rep_events, rep_neurons = rn.replacement_count()
     sup32 = [sorted(x) for x in rn.synapse_list(1)]
     eng.set_kernel_timing(True)
     rn.run_growth_trials(args.warmup + args.steps, 1, True)
@@ -518,6 +526,8 @@ def run_growth(args, local_rank):
                                      "delays mean 3 ms capped 10 ms, 10 training neurons", "trial_ms": trial_ms},
               "neuron_steps_per_s": args.steps / wall * (N_RA + N_I) * (args.num_steps - 1),
               "gpu_launches": launches, "clocks": clk.summary(),
+              "replacements": {"events": rep_events, "neurons": rep_neurons,
+                               "supersynapses_at_end": sum(len(x) for x in sup32)},
               "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()}}
     if not args.skip_fp64:
         eng64 = Engine(precision=64, device=local_rank, use_graphs=False)

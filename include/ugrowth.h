@@ -233,6 +233,9 @@ ug_status ug_get_network_info(ug_ctx* ctx, int32_t net_id, ug_network_info* info
 ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out);
 /* Training neurons and their spread times, [n_tr] each. */
 ug_status ug_get_training(ug_ctx* ctx, int32_t net_id, int32_t* neurons, double* spread);
+/* Replacements since the network was loaded: trials after which replace_neurons
+ * (NetworkGrowthSimulator.cpp:15869-15881) ran, and the neurons it replaced in all. */
+ug_status ug_get_replacement_count(ug_ctx* ctx, int32_t net_id, int64_t* events, int64_t* neurons);
 
 /* ---- Per-neuron traces (set_recording, NetworkGrowthSimulator.cpp:2352-2407) -------------
  * The listed neurons (at most 1024 of each kind) record their state before every step of

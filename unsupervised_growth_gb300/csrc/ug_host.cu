@@ -185,6 +185,7 @@ public:
     virtual ug_status trace(int which, int k, double* out, cudaStream_t st) = 0;
     std::vector<int> trace_ra_ids, trace_i_ids;
     bool traced = false;   // a trial has run since the recording was set
+    int64_t replacement_events = 0, replaced_neurons = 0;   // since the network was loaded
     NetHost h;
     std::vector<int> replaced;      // neurons replaced after the last growth trial
     std::vector<double> T;          // internal_time after step s
@@ -1093,6 +1094,8 @@ ug_status NetImpl<R>::loop_outcome(uint32_t& trial, int& left, cudaStream_t st)
         if (cnt) UG_CUDA(cudaMemcpy(rep.data(), gRep_.as<int>(), cnt * sizeof(int), cudaMemcpyDeviceToHost));
         UG_TRY(pull_bookkeeping(st));
         replaced = rep;
+        replacement_events += 1;
+        replaced_neurons += (int64_t)rep.size();
         UG_TRY(replace_neurons(rep, trial - 1, st));
         UG_TRY(push_bookkeeping(st));
     }
@@ -2462,6 +2465,17 @@ ug_status ug_get_activity_history(ug_ctx* ctx, int32_t net_id, int32_t* out)
     for (int i = 0; i < n->h.n_ra; ++i)
         for (int k = 0; k < W; ++k)
             out[(size_t)i * W + k] = n->h.hist[(size_t)i * W + (n->h.hist_head + k) % W];
+    return UG_OK;
+}
+
+ug_status ug_get_replacement_count(ug_ctx* ctx, int32_t net_id, int64_t* events, int64_t* neurons)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    NetBase* n;
+    UG_TRY(get_net(ctx, net_id, &n));
+    if (events) *events = n->replacement_events;
+    if (neurons) *neurons = n->replaced_neurons;
     return UG_OK;
 }
 

@@ -36,7 +36,7 @@ EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_syn
             "ug_topology_get_coordinates", "ug_topology_get_connections", "ug_topology_get_training",
             "ug_topology_write_dir", "ug_topology_free", "ug_create_growth_network_from_topology",
             "ug_create_network_topology", "ug_calibrate_pipes", "ug_probe_bounded_wait", "ug_set_recording",
-            "ug_get_recording", "ug_get_trace", "ug_write_traces"]
+            "ug_get_recording", "ug_get_trace", "ug_write_traces", "ug_get_replacement_count"]
 
 
 class UGError(RuntimeError):
@@ -201,6 +201,7 @@ def load_library(path: str = LIB_PATH):
     L.ug_get_recording.argtypes = [C.c_void_p, C.c_int32, _i32p, C.POINTER(C.c_int32), _i32p, C.POINTER(C.c_int32)]
     L.ug_get_trace.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _f64p, C.POINTER(C.c_int32)]
     L.ug_write_traces.argtypes = [C.c_void_p, C.c_int32, C.c_char_p, C.c_int32]
+    L.ug_get_replacement_count.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.ug_set_inhibition_tracking.argtypes = [vp, C.c_int32, C.c_double]
     L.ug_get_inhibitory_conductance.argtypes = [vp, C.c_int32, _f64p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
     L.ug_write_inhibition_tracking_state.argtypes = [vp, C.c_int32, C.c_char_p, C.c_int32]
@@ -400,6 +401,12 @@ class ResidentNetwork:
         out = np.zeros((n.value, 5 if which == 0 else 4))
         _check(L.ug_get_trace(self.engine.ctx, self.id, which, k, _ptr(out, _f64p), C.byref(n)))
         return out
+
+    def replacement_count(self):
+        """(trials after which neurons were replaced, neurons replaced) since loading."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        _check(self.engine.L.ug_get_replacement_count(self.engine.ctx, self.id, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def write_traces(self, directory: str, trial: int):
         _check(self.engine.L.ug_write_traces(self.engine.ctx, self.id, directory.encode(), trial))
