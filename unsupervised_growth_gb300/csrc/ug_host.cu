@@ -439,6 +439,7 @@ ug_status NetImpl<R>::init_host(const ug_network_desc* d, int spike_cap_per_neur
     rc_.mu_d = (R)H.noise.white_noise_mean_dend;
     rc_.e1 = (R)std::exp(-kTimestep / ug::RAConst::tau);
     rc_.e2 = (R)std::exp(-0.5 * kTimestep / ug::RAConst::tau);
+    ug::philox_key_schedule(H.seed, rc_.ks);
     ic_.dt = (R)kTimestep;
     for (int k = 0; k < 12; ++k) {
         const double hk = k == 0 ? 0.0 : k == 11 ? kTimestep : cnum[k] * kTimestep / cden[k];
@@ -2773,6 +2774,7 @@ extern "C" ug_status ug_run_test_trial_noalloc(ug_ctx* ctx, int32_t net_id, uint
     rc.mu_s = (float)H.noise.white_noise_mean_soma;
     rc.mu_d = (float)H.noise.white_noise_mean_dend;
     rc.e1 = (float)std::exp(-0.02 / ug::RAConst::tau);
+    ug::philox_key_schedule(H.seed, rc.ks);
     rc.e2 = (float)std::exp(-0.01 / ug::RAConst::tau);
     ic.dt = 0.02f;
     const double cnum[12] = {UG_DP_CNUM}, cden[12] = {UG_DP_CDEN};

@@ -57,7 +57,20 @@ struct RAStep {
     R sig_s, sig_d;       // white-noise amplitudes
     R mu_s, mu_d;         // white-noise means
     R e1, e2;             // conductance decay to t+dt and t+dt/2 (exp(-h/5))
+    uint32_t ks[20];      // the network's Philox key schedule (k0, k1 of rounds 0..9), for the packed kernel
 };
+
+// Philox4x32-10 key schedule of a seed: (k0, k1) of each of the ten rounds.
+inline void philox_key_schedule(uint64_t seed, uint32_t* ks)
+{
+    uint32_t k0 = (uint32_t)(seed & 0xffffffffu), k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        ks[2 * r] = k0;
+        ks[2 * r + 1] = k1;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
 
 __device__ __forceinline__ double ra_point(int idx, double)
 {

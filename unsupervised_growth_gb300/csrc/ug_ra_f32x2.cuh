@@ -200,10 +200,31 @@ __device__ __forceinline__ Philox4 philox_wide(uint32_t c0, uint32_t c1, uint32_
     return Philox4{c0, c1, c2, c3};
 }
 
+// The noise value of a word: the 30-point distribution index is (u * 30) >> 32, and
+// index >= k exactly when u >= ceil(k 2^32 / 30), so unsigned comparisons against those
+// bounds pick the value without a multiply.
 __device__ __forceinline__ float ra_point_f(uint32_t u)
 {
-    const int idx = point_index(u);
-    return idx == 0 ? 2.4494897f : idx == 1 ? -2.4494897f : idx <= 10 ? 1.0f : idx <= 19 ? -1.0f : 0.0f;
+    return u < 143165577u ? 2.4494897f : u < 286331154u ? -2.4494897f : u < 1574821342u ? 1.0f
+                                                                   : u < 2863311531u ? -1.0f : 0.0f;
 }
+
+// Philox4x32-10 with the key schedule precomputed (RAStep::ks): the round keys come from
+// the kernel's parameters, so no instruction updates them.
+__device__ __forceinline__ Philox4 philox_sched(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                const uint32_t* ks)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ ks[2 * r];
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ ks[2 * r + 1];
+        c1 = (uint32_t)p1;
+        c3 = (uint32_t)p0;
+        c0 = n0;
+        c2 = n2;
+    }
+    return Philox4{c0, c1, c2, c3};}
 
 }  // namespace ug

@@ -505,8 +505,8 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
             ra_state_check(c1, fl1, fs, fd);
             soma1 |= (uint32_t)fs << (st - s0);
             dend1 |= (uint32_t)fd << (st - s0);
-            const Philox4 w0 = philox_wide((uint32_t)(st - 1), sid0.entity, sid0.trial, sid0.tag, sid0.k0, sid0.k1);
-            const Philox4 w1 = philox_wide((uint32_t)(st - 1), ent1, sid0.trial, sid0.tag, sid0.k0, sid0.k1);
+            const Philox4 w0 = philox_sched((uint32_t)(st - 1), sid0.entity, sid0.trial, sid0.tag, rc.ks);
+            const Philox4 w1 = philox_sched((uint32_t)(st - 1), ent1, sid0.trial, sid0.tag, rc.ks);
             ra_debrabant_x2(s, Ge, Gi, P, rc, make_float2(ra_point_f(w0.x), ra_point_f(w1.x)),
                             make_float2(ra_point_f(w0.y), ra_point_f(w1.y)), make_float2(ra_point_f(w0.z), ra_point_f(w1.z)),
                             make_float2(ra_point_f(w0.w), ra_point_f(w1.w)));
