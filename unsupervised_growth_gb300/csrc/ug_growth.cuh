@@ -1185,17 +1185,27 @@ __global__ void __launch_bounds__(kEpiWarps * 32) k_growth_epilogue_bulk(GrowthD
         const int j0 = (int)(t % nch) * kEpiChunk;
         const int cnt = min(kEpiChunk, n - j0);
         EpiBuf& B = buf[t & 1];
+        // decay the whole chunk first (its 16 steps are independent), then run
+        // update_synapse on the pairs that can change, in target order
+        unsigned mine = 0;
+#pragma unroll
         for (int k = 0; k < kEpiChunk / 32; ++k) {
             const int c = 32 * k + lane;
             bool change = false;
             if (c < cnt) B.w[c] = epi_decay(B.w[c], sp, B.act[c] != 0, B.sup[c] != 0, &change);
-            unsigned m = __ballot_sync(0xffffffffu, change);
-            if (lane == 0)
-                while (m) {
-                    const int bit = __ffs(m) - 1;
-                    m &= m - 1;
-                    g_update_synapse_w(g, b, i, j0 + 32 * k + bit, B.w[32 * k + bit]);
-                }
+            mine |= (unsigned)change << k;
+        }
+        if (__any_sync(0xffffffffu, mine != 0)) {
+            __syncwarp();   // every lane's decayed weights are visible to lane 0
+            for (int k = 0; k < kEpiChunk / 32; ++k) {
+                unsigned m = __ballot_sync(0xffffffffu, (mine >> k) & 1u);
+                if (lane == 0)
+                    while (m) {
+                        const int bit = __ffs(m) - 1;
+                        m &= m - 1;
+                        g_update_synapse_w(g, b, i, j0 + 32 * k + bit, B.w[32 * k + bit]);
+                    }
+            }
         }
         fence_proxy_async_smem();   // the decayed weights, written by every lane, to the copy engine
         __syncwarp();
