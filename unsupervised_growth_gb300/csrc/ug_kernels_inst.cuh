@@ -27,15 +27,21 @@ inline void launch_noise_events(const NetDev<float>& n, const BatchDev<float>& b
     if (lc.timer) lc.timer->end(lc.main);
 }
 
+// Threads per block of the double-precision integrators: one warp per block for small
+// batches, so that a single trial spreads over as many SMs as it has warps (GB300's FP64
+// pipe is narrow, and a trial of 2000 neurons is only 63 + 18 warps).
+inline int dp_block(int B) { return B < 16 ? 32 : kBlock; }
+
 inline void launch_i(const NetDev<double>& n, const BatchDev<double>& b, int q, int s0, int s1,
                      const IStep<double>& ic, cudaStream_t st, const LaunchCtx& lc)
 {
     if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
-    const dim3 g((n.n_i + kBlock - 1) / kBlock, b.B);
+    const int t = dp_block(b.B);
+    const dim3 g((n.n_i + t - 1) / t, b.B);
     if (b.trace_i)
-        k_interval_i<double, true><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+        k_interval_i<double, true><<<g, t, 0, st>>>(n, b, q, s0, s1, ic);
     else
-        k_interval_i<double><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
+        k_interval_i<double><<<g, t, 0, st>>>(n, b, q, s0, s1, ic);
     if (lc.timer) lc.timer->end(lc.main);
 }
 
@@ -65,12 +71,13 @@ cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, const La
 inline void launch_ra(const NetDev<double>& n, const BatchDev<double>& b, int q, int s0, int s1,
                       const RAStep<double>& rc, const LaunchCtx& lc)
 {
-    const dim3 g((n.n_ra + kBlock - 1) / kBlock, b.B);
+    const int t = dp_block(b.B);
+    const dim3 g((n.n_ra + t - 1) / t, b.B);
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
     if (b.ginh_slot || b.trace_ra)
-        k_interval_ra<double, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+        k_interval_ra<double, true><<<g, t, 0, lc.main>>>(n, b, q, s0, s1, rc);
     else
-        k_interval_ra<double><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);
+        k_interval_ra<double><<<g, t, 0, lc.main>>>(n, b, q, s0, s1, rc);
     if (lc.timer) lc.timer->end(lc.main);
 }
 

@@ -367,7 +367,7 @@ template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                  const RAStep<R>& rc, int bx, int b)
 {
-    const int i = bx * kBlock + threadIdx.x;
+    const int i = bx * (int)blockDim.x + (int)threadIdx.x;
     const bool valid = i < n.n_ra;
     uint32_t soma = 0, dend = 0;
     if (valid) {
@@ -683,7 +683,7 @@ template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
                                                 const IStep<R>& ic, int bx, int b)
 {
-    const int i = bx * kBlock + threadIdx.x;
+    const int i = bx * (int)blockDim.x + (int)threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
