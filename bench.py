@@ -511,8 +511,19 @@ def run_growth(args, local_rank):
     launches = eng.launch_count() - l0
     rep_events, rep_neurons = rn.replacement_count()
     sup32 = [sorted(x) for x in rn.synapse_list(1)]
-    eng.set_kernel_timing(True)
-    rn.run_growth_trials(args.warmup + args.steps, 1, True)
+    # the same network's next trials with per-interval launches (the shape the one-launch
+    # trial replaces), for comparison
+    eng.set_growth_launch(False)
+    n_cmp = 3
+    rn.run_growth_trials(args.warmup + args.steps, 1, True)   # captures that shape's graph
+    eng.synchronize()
+    t0 = time.perf_counter()
+    rn.run_growth_trials(args.warmup + args.steps + 1, n_cmp, True)
+    eng.synchronize()
+    per_interval = n_cmp / (time.perf_counter() - t0)
+    eng.set_growth_launch(True)
+    eng.set_kernel_timing(True)   # kernel timing runs the per-interval launches, one kernel at a time
+    rn.run_growth_trials(args.warmup + args.steps + 1 + n_cmp, 1, True)
     names = ("k_interval_ra", "k_interval_i", "k_growth_rows", "k_growth_newpost", "k_growth_ltp",
              "k_growth_epilogue", "k_trial_init", "k_noise_events", "k_growth_reset")
     kt = {k: eng.kernel_timing(k) for k in names}
@@ -528,9 +539,13 @@ def run_growth(args, local_rank):
               "gpu_launches": launches, "clocks": clk.summary(),
               "replacements": {"events": rep_events, "neurons": rep_neurons,
                                "supersynapses_at_end": sum(len(x) for x in sup32)},
-              "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()}}
+              "launch": "one cooperative kernel per trial (all sync intervals, bounded grid barriers)",
+              "per_interval_launches_trials_per_s": per_interval,
+              "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()},
+              "kernel_ms_how": "per-interval launches timed one kernel at a time"}
     if not args.skip_fp64:
         eng64 = Engine(precision=64, device=local_rank, use_graphs=False)
+        eng64.set_growth_launch(False)   # the plain path: per-interval launches, no graph
         rn64 = eng64.load_network(net)
         t0 = time.perf_counter()
         rn64.run_growth_trials(0, args.warmup + args.steps, True)
@@ -557,6 +572,7 @@ def _fp64_plain_seconds(nets, device, kind):
     no graph) for each network."""
     from unsupervised_growth_gb300.engine import Engine
     eng = Engine(precision=64, device=device, use_graphs=False)
+    eng.set_growth_launch(False)   # the plain path: per-interval launches, no graph
     out = []
     for net in nets:
         rn = eng.load_network(net)

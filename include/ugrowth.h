@@ -152,6 +152,15 @@ ug_status ug_run_group(ug_ctx* ctx, ug_group_item* items, int32_t n_items);
  * interneuron kernel runs beside the HVC(RA) kernel on a second stream (overlap 1) or after
  * it (0).  Results do not depend on the shape. */
 ug_status ug_set_group_launch(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_blocks_per_sm, int32_t overlap);
+/* Launch shape of single-network growth trials (ug_run_growth_trials), no counterpart in the
+ * reference, whose loop over sync intervals is NetworkGrowthSimulator.cpp:8923-9564.
+ * one_launch 1 (the default): each trial's intervals run in one cooperative kernel with
+ * bounded grid barriers between phases, when the network's blocks can all be resident at
+ * once (else, and while recording traces or inhibition, the per-interval launches run);
+ * a barrier not reached within about a second ends the trial with UG_ETIMEOUT.
+ * 0: the per-interval launches (several kernels per sync interval).  Results are the
+ * same bits either way. */
+ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch);
 /* Serving loop -- no counterpart in the reference.  A scheduler thread of the context
  * runs group rounds (see ug_run_group) over the requests on the GPU and, between
  * rounds, admits queued requests in arrival order while their device footprint fits
@@ -418,11 +427,12 @@ ug_status ug_create_network_topology(ug_ctx* ctx, const char* config_file, const
 ug_status ug_calibrate_pipes(int32_t device, double* mufu_ops_per_s, double* fma_ops_per_s);
 
 /* No counterpart in the reference (failure detection).  Every wait in the library's kernels
- * (on an mbarrier of the bulk copy engine, or on a flag in global memory) gives up after
- * one second and raises UG_ETIMEOUT instead of hanging the device.  This runs one such wait
- * that nothing can satisfy -- which 0: a global flag nothing sets; which 1: an mbarrier
- * expecting bytes no copy delivers -- and returns UG_ETIMEOUT once it gives up; the device
- * stays usable. */
+ * (on an mbarrier of the bulk copy engine, on a flag in global memory, or at a grid barrier
+ * of the one-launch growth trial) gives up after one second and raises UG_ETIMEOUT instead
+ * of hanging the device.  This runs one such wait that nothing can satisfy -- which 0: a
+ * global flag nothing sets; which 1: an mbarrier expecting bytes no copy delivers; which 2:
+ * a grid barrier of a two-block cooperative launch that the blocks never reach -- and
+ * returns UG_ETIMEOUT once it gives up; the device stays usable. */
 ug_status ug_probe_bounded_wait(int32_t device, int32_t which);
 
 #ifdef __cplusplus

@@ -1,8 +1,9 @@
 """Failure detection without a GPU fault: every wait in the library's kernels is bounded.
-A wait that nothing can satisfy -- on a global flag nothing sets, or on an mbarrier of the
-bulk copy engine expecting bytes no copy delivers (the wait the growth epilogue uses) --
-gives up after about a second and raises UG_ETIMEOUT, and the device stays usable: a test
-trial run right after gives the oracle's spikes."""
+A wait that nothing can satisfy -- on a global flag nothing sets, on an mbarrier of the
+bulk copy engine expecting bytes no copy delivers (the wait the growth epilogue uses), or
+at a grid barrier of a cooperative launch that its blocks never reach (the barrier of the
+one-launch growth trial) -- gives up after about a second and raises UG_ETIMEOUT, and the
+device stays usable: a test trial run right after gives the oracle's spikes."""
 import time
 
 import numpy as np
@@ -14,7 +15,7 @@ from tests.helpers import oracle_trial_spikes, small_chain, sorted_spikes
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("which", [0, 1])
+@pytest.mark.parametrize("which", [0, 1, 2])
 def test_unsatisfiable_wait_times_out_and_device_stays_usable(which, engine64):
     from unsupervised_growth_gb300.engine import probe_bounded_wait
     t0 = time.perf_counter()

@@ -110,4 +110,55 @@ __device__ __forceinline__ bool flag_wait_bounded(const volatile int* flag)
     return true;
 }
 
+// Thread 0 of the block waits until *word >= value, for at most kWaitNs, or until another
+// block has set `timeout_bit` in *error (it gave up first); then the whole block learns the
+// outcome.  On giving up the block sets the bit itself, so every block of the launch
+// leaves within about one wait.
+__device__ __forceinline__ bool block_wait_geq(const unsigned* word, unsigned value, int* error, int timeout_bit)
+{
+    __shared__ int s_ok;
+    __syncthreads();   // every thread has read the previous outcome
+    if (threadIdx.x == 0) {
+        bool ok = true;
+        const uint64_t t0 = globaltimer_ns();
+        while (*(const volatile unsigned*)word < value) {
+            if ((*(volatile int*)error & timeout_bit) || globaltimer_ns() - t0 > kWaitNs) {
+                ok = false;
+                break;
+            }
+            __nanosleep(32);
+        }
+        if (!ok) atomicOr(error, timeout_bit);
+        __threadfence();   // what the releasing blocks wrote is read after this
+        s_ok = ok ? 1 : 0;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Grid-wide barrier of a cooperative launch.  `count` counts arrivals; barrier k of the
+// launch is passed once it reaches k * gridDim.x.  Each block's writes are fenced before
+// its arrival and read after the wait, so everything written before the barrier is seen
+// after it.  Bounded: false (with `timeout_bit` set in *error) if the others did not
+// arrive within kWaitNs.
+__device__ __forceinline__ bool grid_barrier_bounded(unsigned* count, unsigned k, int* error, int timeout_bit)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+    }
+    return block_wait_geq(count, k * gridDim.x, error, timeout_bit);
+}
+
+// The block's writes so far, published to blocks that wait for *word >= value.
+__device__ __forceinline__ void block_release(unsigned* word, unsigned value)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicMax(word, value);
+    }
+}
+
 }  // namespace ug

@@ -54,13 +54,18 @@ __global__ void k_fma_loop(float* out, int iters, float seed)
 
 // A wait that nothing can satisfy, bounded like every wait of the library: which 0 polls
 // a global flag nothing sets; which 1 waits on an mbarrier that expects 16 bytes of
-// transactions no copy delivers.  error[0] gets 8 (the timeout flag) once it gives up.
-__global__ void k_wait_probe(int which, const int* flag, int* error)
+// transactions no copy delivers; which 2 is the grid barrier of the one-launch growth
+// trial (a cooperative launch of two blocks) waiting for its second barrier, which the
+// blocks never reach.  error[0] gets 8 (the timeout flag) once it gives up.
+__global__ void k_wait_probe(int which, int* flag, int* error)
 {
     __shared__ uint64_t bar;
     bool ok;
     if (which == 0) {
         ok = ug::flag_wait_bounded(flag);
+    } else if (which == 2) {
+        // one arrival per block, but the wait is for the second barrier (2 x 2 arrivals)
+        ok = ug::grid_barrier_bounded(reinterpret_cast<unsigned*>(flag), 2u, error, 8);
     } else {
         if (threadIdx.x == 0) {
             ug::mbar_init(&bar, 1);
@@ -77,15 +82,26 @@ __global__ void k_wait_probe(int which, const int* flag, int* error)
 
 extern "C" ug_status ug_probe_bounded_wait(int32_t device, int32_t which)
 {
-    if (which != 0 && which != 1) return UG_EINVAL;
+    if (which < 0 || which > 2) return UG_EINVAL;
     if (cudaSetDevice(device) != cudaSuccess) return UG_ECUDA;
     int* buf = nullptr;
     if (cudaMalloc(&buf, 2 * sizeof(int)) != cudaSuccess) return UG_ENOMEM;
     int host[2] = {0, 0};
     cudaError_t e = cudaMemset(buf, 0, 2 * sizeof(int));
     if (e == cudaSuccess) {
-        k_wait_probe<<<1, 32>>>(which, buf, buf + 1);
-        e = cudaDeviceSynchronize();
+        if (which == 2) {
+            int coop = 0;
+            e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+            if (e == cudaSuccess && !coop) e = cudaErrorNotSupported;
+            int w = which;
+            int* f = buf;
+            int* err = buf + 1;
+            void* args[] = {&w, &f, &err};
+            if (e == cudaSuccess) e = cudaLaunchCooperativeKernel((const void*)k_wait_probe, dim3(2), dim3(64), args, 0, 0);
+        } else {
+            k_wait_probe<<<1, 32>>>(which, buf, buf + 1);
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
     if (e == cudaSuccess) e = cudaMemcpy(host, buf, sizeof(host), cudaMemcpyDeviceToHost);
     cudaFree(buf);

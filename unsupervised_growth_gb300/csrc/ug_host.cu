@@ -322,6 +322,15 @@ private:
     DevMem gHist_, gHead_, gHsum_, gHact_, gFrl_, gScale_, gMatf_, gRest_, gGca_, gMature_, gTar_, gRepCnt_, gLoop_;
     ug::TailDev<R> td_{};
     bool book_dirty_ = false;      // the device bookkeeping changed since the host copy was read
+    // the one-launch growth trial (ug_growth_trial.cuh)
+    DevMem gTrialCtl_, gActRows_, gSyncEnd_;   // barrier and queue words, row queue, sync steps
+    int trial_blocks_ = 0;         // its grid (0: the network's blocks cannot all be resident)
+    int gloop_trial_launch_ = -1;  // the mode the loop graph was captured with
+    bool one_launch(const ug::LaunchCtx& lc) const
+    {
+        return lc.trial_launch && !lc.timer && trial_blocks_ > 0 && bd_.B == 1 && !bd_.trace_ra && !bd_.trace_i &&
+               !bd_.ginh_slot;
+    }
     DevMem gTrRaSlot_, gTrISlot_, gTrRaBuf_, gTrIBuf_;   // per-neuron traces
     void apply_recording()
     {
@@ -927,6 +936,17 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     UG_TRY(gRepCnt_.alloc(sizeof(int)));
     UG_TRY(gLoop_.alloc(ug::kLoopWords * sizeof(int)));
     if (!hloop_) UG_CUDA(cudaMallocHost(&hloop_, ug::kLoopWords * sizeof(int)));
+    // the one-launch trial: barrier and queue words, the row queue, the sync steps
+    UG_TRY(gTrialCtl_.alloc(8 * sizeof(unsigned)));
+    UG_TRY(gActRows_.alloc(4 * (size_t)n * sizeof(int2)));
+    UG_TRY(gSyncEnd_.upload(sync_steps, st));
+    trial_blocks_ = 0;
+    bool fits = !sync_steps.empty();
+    for (size_t q = 0; q < sync_steps.size(); ++q) {
+        const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
+        if (sync_steps[q] - s0 >= ug::kSegSteps) fits = false;
+    }
+    if (fits) UG_CUDA(ug::growth_trial_grid<R>(h.n_ra, h.n_i, &trial_blocks_));
     ug::TailDev<R>& t = td_;
     t.n = n;
     t.W = win;
@@ -1013,17 +1033,40 @@ ug_status NetImpl<R>::issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launc
     UG_CUDA(ug::launch_growth_reset<R>(gd_, lc));
     ++cnt;
     const int Q = (int)sync_steps.size();
-    bool tail_open = false;
-    for (int q = 0; q < Q; ++q) {
-        const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
-        UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, lc));
-        UG_CUDA(ug::launch_growth_sync<R>(gd_, nd_, bd_, q, s0, sync_steps[q], lc, tail_open));
-        cnt += 5;
+    if (one_launch(lc)) {
+        // every interval in one cooperative launch; its queue of rows with deliveries
+        unsigned* ctl = gTrialCtl_.as<unsigned>();
+        UG_CUDA(cudaMemsetAsync(ctl, 0, gTrialCtl_.bytes(), lc.main));
+        ug::BatchDev<R> b = bd_;
+        b.act_rows = gActRows_.as<int2>();
+        b.act_cnt = reinterpret_cast<int*>(ctl + 4);
+        b.act_cap = h.n_ra;
+        b.member = 0;
+        b.live_streams = gd_.st_num;
+        b.heavy = 0;
+        ug::TrialLoop L;
+        L.sync_end = gSyncEnd_.as<int>();
+        L.Q = Q;
+        int nb_sync = 0;
+        ug::trial_roles<R>(h.n_ra, h.n_i, &L.nb_ra, &L.nb_i, &nb_sync);
+        L.bar = ctl;
+        L.posted = ctl + 1;
+        UG_CUDA(ug::launch_growth_trial<R>(gd_, nd_, b, rc_, ic_, L, trial_blocks_, lc.main));
+        cnt += 1;
+    } else {
+        bool tail_open = false;
+        for (int q = 0; q < Q; ++q) {
+            const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
+            UG_CUDA(ug::launch_interval<R>(nd_, bd_, q, s0, sync_steps[q], rc_, ic_, lc));
+            UG_CUDA(ug::launch_growth_sync<R>(gd_, nd_, bd_, q, s0, sync_steps[q], lc, tail_open));
+            cnt += 5;
+        }
+        UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
+        UG_CUDA(ug::launch_tail_join(lc, tail_open));
+        cnt += 2;
     }
-    UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
-    UG_CUDA(ug::launch_tail_join(lc, tail_open));
     UG_CUDA(ug::launch_growth_epilogue<R>(gd_, lc));
-    cnt += 3;
+    ++cnt;
     if (launches) *launches += cnt;
     return UG_OK;
 }
@@ -1042,12 +1085,16 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
     UG_TRY(prepare_growth_run(training, st));
     uint32_t trial = first_trial;
     int left = n_trials;
-    const int64_t per_trial = 2 + (sizeof(R) == 4 ? 1 : 0) + 5 * (int64_t)sync_steps.size() + 2 + 3;
+    // kernels per trial: head, the trial (issue_growth_trial), check_bad_values, tail
+    const int64_t per_trial = 2 + (sizeof(R) == 4 ? 1 : 0) + 1 +
+                              (one_launch(lc) ? 1 : 5 * (int64_t)sync_steps.size() + 2) + 1 + 2;
     while (left > 0) {
         const int words[ug::kLoopWords] = {left, (int)trial, ug::kLoopRunning, 0};
         UG_CUDA(cudaMemcpyAsync(gLoop_.as<int>(), words, sizeof(words), cudaMemcpyHostToDevice, st));
         if (graphs && !lc.timer) {
-            if (!gloop_ || gloop_training_ != bd_.kick_on || gloop_ginh_gen_ != ginh_gen_) UG_TRY(capture_growth_loop(lc));
+            if (!gloop_ || gloop_training_ != bd_.kick_on || gloop_ginh_gen_ != ginh_gen_ ||
+                gloop_trial_launch_ != lc.trial_launch)
+                UG_TRY(capture_growth_loop(lc));
             UG_CUDA(cudaGraphLaunch(gloop_, st));
             UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost, st));
             UG_CUDA(cudaStreamSynchronize(st));
@@ -1057,7 +1104,7 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
                 ug::TailDev<R> t = td_;
                 t.has_cond = 0;
                 UG_CUDA(ug::launch_growth_head<R>(t, gBad_.as<int>(), st));
-                UG_TRY(issue_growth_trial(lc, launches));
+                UG_TRY(issue_growth_trial(lc, nullptr));   // counted with per_trial below
                 UG_CUDA(ug::launch_check_bad<R>(nd_, bd_, gBad_.as<int>(), st));
                 UG_CUDA(ug::launch_growth_tail<R>(t, st));
                 UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost,
@@ -1157,6 +1204,7 @@ ug_status NetImpl<R>::capture_growth_loop(const ug::LaunchCtx& lc)
     UG_CUDA(e);
     gloop_training_ = bd_.kick_on;
     gloop_ginh_gen_ = ginh_gen_;
+    gloop_trial_launch_ = lc.trial_launch;
     return UG_OK;
 }
 
@@ -1809,6 +1857,7 @@ struct ug_ctx {
         lc.tail_fork = tail_fork;
         lc.tail_join = tail_join;
         lc.timer = timer.enabled ? &timer : nullptr;
+        lc.trial_launch = trial_launch;
         return lc;
     }
     int64_t launches = 0;
@@ -1817,6 +1866,7 @@ struct ug_ctx {
     std::unique_ptr<GroupBase> group;          // GroupExec<float> or GroupExec<double>
     int group_ra_bps = 0, group_i_bps = 0;     // integrator blocks per SM of group launches (0: occupancy)
     int group_overlap = 1;                     // interneuron kernel beside the RA kernel
+    int trial_launch = 1;                      // growth trials of one network in one cooperative launch
     std::recursive_mutex mu;                   // one caller at a time: API calls and the server's rounds
     std::unique_ptr<Server> server;
     ~ug_ctx();
@@ -2290,6 +2340,14 @@ ug_status ug_set_group_launch(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_b
     ctx->group_ra_bps = ra_blocks_per_sm;
     ctx->group_i_bps = i_blocks_per_sm;
     ctx->group_overlap = overlap ? 1 : 0;
+    return UG_OK;
+}
+
+ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    ctx->trial_launch = one_launch ? 1 : 0;
     return UG_OK;
 }
 

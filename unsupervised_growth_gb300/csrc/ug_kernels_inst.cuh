@@ -171,6 +171,47 @@ cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc)
     return cudaGetLastError();
 }
 
+// Dynamic shared memory of k_growth_trial: one row buffer per warp.
+constexpr size_t kTrialSmem = (size_t)kTrialWarps * sizeof(RowShared);
+
+template <class R>
+cudaError_t growth_trial_grid(int n_ra, int n_i, int* blocks)
+{
+    *blocks = 0;
+    cudaError_t e =
+        cudaFuncSetAttribute(k_growth_trial<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrialSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0, coop = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_growth_trial<R>, kTrialThreads, kTrialSmem);
+    if (e != cudaSuccess) return e;
+    int nb_ra = 0, nb_i = 0, nb_sync = 0;
+    trial_roles<R>(n_ra, n_i, &nb_ra, &nb_i, &nb_sync);
+    const long long total = (long long)nb_ra + nb_i + nb_sync;
+    if (coop && per_sm > 0 && total <= (long long)per_sm * sms) *blocks = (int)total;
+    return cudaSuccess;
+}
+
+template <class R>
+cudaError_t launch_growth_trial(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, const RAStep<R>& rc,
+                                const IStep<R>& ic, const TrialLoop& L, int blocks, cudaStream_t st)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(kTrialThreads);
+    cfg.dynamicSmemBytes = kTrialSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;   // every block resident at once, or the launch fails
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_growth_trial<R>, g, n, b, rc, ic, L);
+}
+
 // Grid of the bulk-copy epilogue for B networks of n neurons (0: rows not 16-byte aligned
 // in every array, so the warp epilogue runs), after allowing its shared memory.
 template <class R>

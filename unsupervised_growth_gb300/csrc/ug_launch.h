@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "ug_group.cuh"
+#include "ug_growth_trial.cuh"
 #include "ug_tail.cuh"
 
 namespace ug {
@@ -97,6 +98,9 @@ struct LaunchCtx {
     cudaStream_t tail = nullptr;
     cudaEvent_t tail_fork = nullptr, tail_join = nullptr;
     KernelTimer* timer = nullptr;
+    // growth: the whole trial in one cooperative launch (k_growth_trial) where the
+    // network's blocks can all be resident; 0 keeps the per-interval launches
+    int trial_launch = 1;
 };
 
 template <class R>
@@ -123,6 +127,13 @@ inline cudaError_t launch_tail_join(const LaunchCtx& lc, bool& tail_open)
 }
 template <class R>
 cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc);
+// The one-launch growth trial (ug_growth_trial.cuh): its grid for a network (0 when the
+// blocks cannot all be resident at once), and the cooperative launch.
+template <class R>
+cudaError_t growth_trial_grid(int n_ra, int n_i, int* blocks);
+template <class R>
+cudaError_t launch_growth_trial(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, const RAStep<R>& rc,
+                                const IStep<R>& ic, const TrialLoop& L, int blocks, cudaStream_t st);
 template <class R>
 cudaError_t launch_growth_remove(const GrowthDev& g, const int* rep, int nrep, cudaStream_t st);
 template <class R>

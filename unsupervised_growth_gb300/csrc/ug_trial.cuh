@@ -365,9 +365,10 @@ __global__ void __launch_bounds__(kBlock) k_trial_init(NetDev<R> n, BatchDev<R> 
 // integrators without tracking carry none of it).
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                 const RAStep<R>& rc, int bx, int b)
+                                                 const RAStep<R>& rc, int bx, int b, int width = 0)
 {
-    const int i = bx * (int)blockDim.x + (int)threadIdx.x;
+    // width: neurons of a block (the block's first `width` threads take part; 0: all)
+    const int i = bx * (width ? width : (int)blockDim.x) + (int)threadIdx.x;
     const bool valid = i < n.n_ra;
     uint32_t soma = 0, dend = 0;
     if (valid) {
@@ -681,9 +682,9 @@ __global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev
 // HVC(I) part of one interval; scatters the I->RA kicks of its spikes.
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                const IStep<R>& ic, int bx, int b)
+                                                const IStep<R>& ic, int bx, int b, int width = 0)
 {
-    const int i = bx * (int)blockDim.x + (int)threadIdx.x;
+    const int i = bx * (width ? width : (int)blockDim.x) + (int)threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
