@@ -492,42 +492,59 @@ def run_growth(args, local_rank):
     double-precision weights, against the plain double-precision path."""
     import torch
 
+    from unsupervised_growth_gb300 import autotune
     from unsupervised_growth_gb300 import build as B
     from unsupervised_growth_gb300.engine import Engine
     B.build()
     torch.cuda.set_device(local_rank)
     net = make_growth_network(num_steps=args.num_steps)
-    eng = Engine(precision=32, device=local_rank)
+    eng = Engine(precision=32, device=local_rank, use_graphs=not args.no_graphs)
     rn = eng.load_network(net)
     rn.run_growth_trials(0, args.warmup, True)
     eng.synchronize()
     eng.set_kernel_timing(False)
+    # the block shape of the one-launch trial, tuned on the run's own next trials
+    nxt = [args.warmup]
+
+    def one_trial():
+        rn.run_growth_trials(nxt[0], 1, True)
+        eng.synchronize()
+        nxt[0] += 1
+
+    cache = autotune.DEFAULT_CACHE if args.autotune_cache is None else (args.autotune_cache or None)
+    tuned = autotune.tune_growth_trial(eng, one_trial,
+                                       sig=autotune.trial_signature(_device_name(local_rank), N_RA, N_I, 32),
+                                       cache_path=cache)
+    first = nxt[0]
     l0 = eng.launch_count()
     with ClockSampler(local_rank) as clk:
         t0 = time.perf_counter()
-        rn.run_growth_trials(args.warmup, args.steps, True)
+        rn.run_growth_trials(first, args.steps, True)
         eng.synchronize()
         wall = time.perf_counter() - t0
     launches = eng.launch_count() - l0
     rep_events, rep_neurons = rn.replacement_count()
     sup32 = [sorted(x) for x in rn.synapse_list(1)]
-    # the same network's next trials with per-interval launches (the shape the one-launch
-    # trial replaces), for comparison
-    eng.set_growth_launch(False)
-    n_cmp = 3
-    rn.run_growth_trials(args.warmup + args.steps, 1, True)   # captures that shape's graph
-    eng.synchronize()
-    t0 = time.perf_counter()
-    rn.run_growth_trials(args.warmup + args.steps + 1, n_cmp, True)
-    eng.synchronize()
-    per_interval = n_cmp / (time.perf_counter() - t0)
-    eng.set_growth_launch(True)
-    eng.set_kernel_timing(True)   # kernel timing runs the per-interval launches, one kernel at a time
-    rn.run_growth_trials(args.warmup + args.steps + 1 + n_cmp, 1, True)
-    names = ("k_interval_ra", "k_interval_i", "k_growth_rows", "k_growth_newpost", "k_growth_ltp",
-             "k_growth_epilogue", "k_trial_init", "k_noise_events", "k_growth_reset")
-    kt = {k: eng.kernel_timing(k) for k in names}
-    eng.set_kernel_timing(False)
+    per_interval, kt = None, {}
+    if not args.skip_compare:
+        # the same network's next trials with per-interval launches (the shape the
+        # one-launch trial replaces), for comparison
+        eng.set_growth_launch(False)
+        n_cmp = 3
+        nxt = first + args.steps
+        rn.run_growth_trials(nxt, 1, True)   # captures that shape's graph
+        eng.synchronize()
+        t0 = time.perf_counter()
+        rn.run_growth_trials(nxt + 1, n_cmp, True)
+        eng.synchronize()
+        per_interval = n_cmp / (time.perf_counter() - t0)
+        eng.set_growth_launch(True)
+        eng.set_kernel_timing(True)   # kernel timing runs the per-interval launches, one kernel at a time
+        rn.run_growth_trials(nxt + 1 + n_cmp, 1, True)
+        names = ("k_interval_ra", "k_interval_i", "k_growth_rows", "k_growth_newpost", "k_growth_ltp",
+                 "k_growth_epilogue", "k_trial_init", "k_noise_events", "k_growth_reset")
+        kt = {k: eng.kernel_timing(k) for k in names}
+        eng.set_kernel_timing(False)
     trial_ms = (args.num_steps - 1) * 0.02
     result = {"metric": f"growth trials/s ({trial_ms:g} ms growth trials, 2000 RA + 550 I network, one network)",
               "value": args.steps / wall, "unit": "trials/s", "n_gpus": 1, "steps": args.steps,
@@ -540,6 +557,11 @@ def run_growth(args, local_rank):
               "replacements": {"events": rep_events, "neurons": rep_neurons,
                                "supersynapses_at_end": sum(len(x) for x in sup32)},
               "launch": "one cooperative kernel per trial (all sync intervals, bounded grid barriers)",
+              "trial_shape": {"ra_threads": tuned["shape"][0], "i_threads": tuned["shape"][1],
+                              "cached": tuned["cached"],
+                              "table": [[t["shape"][0], t["shape"][1], round(1e3 * t["seconds"], 2)]
+                                        for t in tuned["table"]],
+                              "how": "autotuned [ra, i, ms per trial]; 0 = default (32 threads)"},
               "per_interval_launches_trials_per_s": per_interval,
               "kernel_ms_per_trial": {k: round(v[0], 3) for k, v in kt.items()},
               "kernel_ms_how": "per-interval launches timed one kernel at a time"}
@@ -908,11 +930,13 @@ def main():
     ap.add_argument("--rate", type=float, default=2.0, help="serve: arrivals per second")
     ap.add_argument("--skip-sequential", action="store_true", help="uneven: skip the one-network-at-a-time timing")
     ap.add_argument("--autotune-cache", default=None,
-                    help="uneven: autotuner cache file ('' to tune every run; default: the package's cache)")
+                    help="uneven, growth: autotuner cache file ('' to tune every run; default: the package's cache)")
     ap.add_argument("--batch", type=int, default=BATCH, help="test trials per step (profiling runs use fewer)")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernels directly instead of graph replay")
     ap.add_argument("--skip-cpu", action="store_true", help="do not time the CPU baseline")
     ap.add_argument("--skip-fp64", action="store_true", help="do not time the plain double-precision GPU path")
+    ap.add_argument("--skip-compare", action="store_true",
+                    help="growth: do not time the per-interval launches and their per-kernel split")
     ap.add_argument("--skip-serve", action="store_true", help="do not run the serving-latency leg of the headline")
     args = ap.parse_args()
     if args.gpus > 1 and "RANK" not in os.environ:

@@ -161,6 +161,15 @@ ug_status ug_set_group_launch(ug_ctx* ctx, int32_t ra_blocks_per_sm, int32_t i_b
  * 0: the per-interval launches (several kernels per sync interval).  Results are the
  * same bits either way. */
 ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch);
+/* Block shape of the one-launch growth trial, no counterpart in the reference (its neurons
+ * step one after another in each rank's loop, NetworkGrowthSimulator.cpp:8923-8950):
+ * integrating threads per block of the HVC(RA) and of the HVC(I) role, each 0 (the default,
+ * 32: one integrating warp per block; the single build's RA threads step two neurons each)
+ * or a multiple of 32 in [32, 256].  Wider roles put a network's neurons on fewer SMs, with
+ * more integrating warps sharing an SM scheduler between two grid barriers.
+ * Results are the same bits for every shape; a shape whose blocks cannot all be resident
+ * runs the per-interval launches.  UG_EINVAL for other widths. */
+ug_status ug_set_growth_trial_shape(ug_ctx* ctx, int32_t ra_threads, int32_t i_threads);
 /* Serving loop -- no counterpart in the reference.  A scheduler thread of the context
  * runs group rounds (see ug_run_group) over the requests on the GPU and, between
  * rounds, admits queued requests in arrival order while their device footprint fits

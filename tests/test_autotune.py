@@ -41,3 +41,34 @@ def test_round_budget_and_signature():
     a = autotune.signature("GB300", [(2000, "growth", 1)] * 64)
     b = autotune.signature("GB300", [(2000, "growth", 1)] * 64 + [(300, "test", 10)])
     assert a != b and a.startswith("GB300|g|m64|")
+
+
+class FakeTrialEngine:
+    def __init__(self, cost):
+        self.cost, self.shape, self.calls = cost, None, 0
+
+    def set_growth_trial_shape(self, ra=0, i=0):
+        self.shape = (ra, i)
+
+    def run_trial(self):
+        self.calls += 1
+        autotune.time.sleep(self.cost(self.shape))
+
+
+def test_growth_trial_shape_descent_and_cache(tmp_path):
+    # fastest: 64-thread HVC(RA) role, 32-thread interneuron role
+    def cost(shape):
+        ra, i = shape
+        return 0.002 + (0.0 if ra == 64 else 0.006) + (0.0 if i == 32 else 0.004)
+
+    eng = FakeTrialEngine(cost)
+    path = str(tmp_path / "cache.json")
+    sig = autotune.trial_signature("GB300", 2000, 550, 32)
+    assert sig == "GB300|trial32|ra10|i9"
+    res = autotune.tune_growth_trial(eng, eng.run_trial, sig=sig, cache_path=path)
+    assert res["shape"] == (64, 32) and eng.shape == (64, 32) and not res["cached"]
+    # every candidate runs one untimed trial (graph capture) and one timed trial
+    assert res["trials"] == 2 * len(res["table"]) == eng.calls
+    eng2 = FakeTrialEngine(cost)
+    res2 = autotune.tune_growth_trial(eng2, eng2.run_trial, sig=sig, cache_path=path)
+    assert res2["cached"] and res2["shape"] == (64, 32) and eng2.calls == 0 and eng2.shape == (64, 32)

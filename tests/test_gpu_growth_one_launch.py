@@ -114,3 +114,30 @@ def test_consecutive_trials_in_one_call_fp32(engine32):
         assert np.array_equal(sorted_spikes(*a.spikes(0, w)), sorted_spikes(*b.spikes(0, w))), w
     a.free()
     b.free()
+
+
+def test_trial_shapes_give_the_same_bits(engine32, engine64):
+    """Every block shape of the one-launch trial (ug_set_growth_trial_shape) gives the
+    default shape's bits: narrower or wider integrating roles, both builds."""
+    net = config2_network(syn=FAST_SYN, mat=FAST_MAT)
+    ref, _ = _run(engine32, net, 2, True)
+    for shape in [(256, 256), (64, 128), (128, 64)]:
+        engine32.set_growth_trial_shape(*shape)
+        try:
+            got, n = _run(engine32, net, 2, True)
+        finally:
+            engine32.set_growth_trial_shape(0, 0)
+        _assert_same(got, ref)
+        assert n <= 10, (shape, n)
+    small = growth_net()
+    ref64, _ = _run(engine64, small, 2, True)
+    engine64.set_growth_trial_shape(64, 96)
+    try:
+        got64, _ = _run(engine64, small, 2, True)
+    finally:
+        engine64.set_growth_trial_shape(0, 0)
+    _assert_same(got64, ref64)
+    with pytest.raises(RuntimeError):
+        engine32.set_growth_trial_shape(48, 0)
+    with pytest.raises(RuntimeError):
+        engine32.set_growth_trial_shape(0, 512)

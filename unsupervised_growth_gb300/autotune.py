@@ -1,4 +1,4 @@
-"""Launch-shape autotuner for group runs and the serving loop.
+"""Launch-shape autotuner for group runs, the serving loop and single-network growth trials.
 
 The group kernels run persistent, occupancy-sized grids over device work lists
 (``ug_run_group``).  Three knobs decide how a round's work meets the SMs: the
@@ -101,3 +101,69 @@ def tune(engine, run_round, sig: str | None = None, cache_path: str | None = DEF
                       "table": table}
         _store(cache_path, cache)
     return {"shape": best_shape, "table": table, "rounds": rounds[0], "cached": False}
+
+
+# Integrating threads per block of the one-launch growth trial's HVC(RA) and HVC(I)
+# roles (ug_set_growth_trial_shape); 0 = the build's default.
+TRIAL_WIDTHS = (256, 128, 64, 32)
+
+
+def trial_signature(device_name: str, n_ra: int, n_i: int, precision: int) -> str:
+    """Signature of a single-network growth run: device, precision and both neuron counts
+    on a log2 scale."""
+    return (f"{device_name}|trial{precision}|ra{int(math.log2(max(n_ra, 1)))}"
+            f"|i{int(math.log2(max(n_i, 1)))}")
+
+
+def tune_growth_trial(engine, run_trial, sig: str | None = None, cache_path: str | None = DEFAULT_CACHE,
+                      widths=TRIAL_WIDTHS, repeats: int = 1):
+    """Chooses the block shape of the one-launch growth trial for `run_trial` (a callable
+    that runs the caller's next growth trial(s) through `engine` and returns when done).
+
+    A single network's trial is a chain of sync intervals separated by grid barriers, so
+    its time is the latency of the slowest block per interval: how many integrating warps
+    share an SM scheduler decides it, not occupancy.  Because an interval waits for the
+    slower of the two roles, narrowing one role alone can show no gain; so the search
+    first tries equal widths for both roles, then refines the HVC(RA) width and then the
+    HVC(I) width from the best of those, keeping each faster shape.  With a cached entry
+    for `sig` the shape is applied without timing.  The results are the same bits for
+    every shape, so the timed trials are ordinary trials of the run.  Returns
+    {"shape", "table", "trials", "cached"}."""
+    cache = _load(cache_path) if (cache_path and sig) else {}
+    if sig and sig in cache:
+        ra, ii = cache[sig]["shape"]
+        engine.set_growth_trial_shape(ra, ii)
+        return {"shape": (ra, ii), "table": cache[sig].get("table", []), "trials": 0, "cached": True}
+    table = []
+    trials = [0]
+
+    def measure(shape):
+        engine.set_growth_trial_shape(*shape)
+        run_trial()   # the first trial of a shape captures its graph
+        trials[0] += 1
+        best = math.inf
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            run_trial()
+            best = min(best, time.perf_counter() - t0)
+            trials[0] += 1
+        table.append({"shape": list(shape), "seconds": best})
+        return best
+
+    best_shape = (0, 0)
+    best_t = measure(best_shape)
+    tried = {best_shape}
+    for knob in ("both", "ra", "i"):
+        for w in widths:
+            cand = (w, w) if knob == "both" else (w, best_shape[1]) if knob == "ra" else (best_shape[0], w)
+            if cand in tried:
+                continue
+            tried.add(cand)
+            t = measure(cand)
+            if t < best_t:
+                best_t, best_shape = t, cand
+    engine.set_growth_trial_shape(*best_shape)
+    if cache_path and sig:
+        cache[sig] = {"shape": list(best_shape), "seconds": best_t, "table": table}
+        _store(cache_path, cache)
+    return {"shape": best_shape, "table": table, "trials": trials[0], "cached": False}

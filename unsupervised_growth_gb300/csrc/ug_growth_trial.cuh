@@ -29,24 +29,41 @@ namespace ug {
 constexpr int kTrialThreads = 256;
 constexpr int kTrialWarps = kTrialThreads / 32;
 
-// Neurons per block of the integrating roles.  The single build's packed integrator
-// steps two HVC(RA) neurons per thread; the double build runs one warp per block (like
-// its per-interval launches), so a trial spreads over as many SMs as it has warps.
+// Threads per block of the integrating roles (whole warps, at most kTrialThreads).  The
+// single build's packed integrator steps two HVC(RA) neurons per thread, its interneuron
+// integrator one; the double build one neuron per thread.  A trial is a chain of
+// intervals whose length is set by the slowest integrating warp, so by default one warp
+// per block integrates (one integrating warp per SM), and a trial spreads over as many
+// SMs as it has integrating warps; wider roles put several integrating warps on one SM
+// scheduler (on the 2000 + 550 network: 98.7 ms per trial at 256 threads, 81.9 ms at 32).
 template <class R>
 struct TrialShape;
 template <>
 struct TrialShape<float> {
-    static constexpr int ra = 2 * kTrialThreads, in = kTrialThreads;
+    static constexpr int ra_w = 32, i_w = 32, ra_per_thread = 2;
 };
 template <>
 struct TrialShape<double> {
-    static constexpr int ra = 32, in = 32;
+    static constexpr int ra_w = 32, i_w = 32, ra_per_thread = 1;
 };
+
+// The role widths of a request (0: the default); false unless each is a multiple of 32
+// in [32, kTrialThreads].
+template <class R>
+__host__ __device__ inline bool trial_widths(int req_ra, int req_i, int* ra_w, int* i_w)
+{
+    *ra_w = req_ra ? req_ra : TrialShape<R>::ra_w;
+    *i_w = req_i ? req_i : TrialShape<R>::i_w;
+    for (int w : {*ra_w, *i_w})
+        if (w < 32 || w > kTrialThreads || w % 32) return false;
+    return true;
+}
 
 struct TrialLoop {
     const int* sync_end;   // [Q] last step of each sync interval
     int Q;                 // sync intervals before the trailing one
     int nb_ra, nb_i;       // blocks of the two integrating roles; the rest are sync blocks
+    int ra_w, i_w;         // integrating threads per block of the two roles
     unsigned* bar;         // grid-barrier arrivals, zero at the launch
     unsigned* posted;      // last interval whose new post events are in place, zero at the launch
 };
@@ -54,32 +71,36 @@ struct TrialLoop {
 // Grid size of k_growth_trial for a network: the three roles, one sync block per
 // kTrialThreads rows.
 template <class R>
-__host__ __device__ inline void trial_roles(int n_ra, int n_i, int* nb_ra, int* nb_i, int* nb_sync)
+__host__ __device__ inline void trial_roles(int n_ra, int n_i, int ra_w, int i_w, int* nb_ra, int* nb_i,
+                                            int* nb_sync)
 {
-    *nb_ra = (n_ra + TrialShape<R>::ra - 1) / TrialShape<R>::ra;
-    *nb_i = (n_i + TrialShape<R>::in - 1) / TrialShape<R>::in;
+    const int ra = TrialShape<R>::ra_per_thread * ra_w;
+    *nb_ra = (n_ra + ra - 1) / ra;
+    *nb_i = (n_i + i_w - 1) / i_w;
     *nb_sync = (n_ra + kTrialThreads - 1) / kTrialThreads;
 }
 
 template <class R>
 __device__ __forceinline__ void trial_ra_part(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                              const RAStep<R>& rc, int k)
+                                              const RAStep<R>& rc, int k, int ra_w)
 {
+    if (threadIdx.x >= ra_w) return;
     if constexpr (sizeof(R) == 4) {
-        interval_ra_x2_body<R>(n, bt, q, s0, s1, rc, 2 * k, 0);   // pairs [256 k, 256 k + 256)
+        interval_ra_x2_body<R>(n, bt, q, s0, s1, rc, k, 0, ra_w);   // pairs [ra_w k, ra_w (k + 1))
     } else {
-        if (threadIdx.x < TrialShape<R>::ra) interval_ra_body<R>(n, bt, q, s0, s1, rc, k, 0, TrialShape<R>::ra);
+        interval_ra_body<R>(n, bt, q, s0, s1, rc, k, 0, ra_w);
     }
 }
 
 template <class R>
 __device__ __forceinline__ void trial_i_part(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                             const IStep<R>& ic, int k)
+                                             const IStep<R>& ic, int k, int i_w)
 {
+    if (threadIdx.x >= i_w) return;
     if constexpr (sizeof(R) == 4) {
-        interval_i_x_body<R>(n, bt, q, s0, s1, ic, 2 * k, 0);      // interneurons [256 k, 256 k + 256)
+        interval_i_x_body<R>(n, bt, q, s0, s1, ic, k, 0, i_w);      // interneurons [i_w k, i_w (k + 1))
     } else {
-        if (threadIdx.x < TrialShape<R>::in) interval_i_body<R>(n, bt, q, s0, s1, ic, k, 0, TrialShape<R>::in);
+        interval_i_body<R>(n, bt, q, s0, s1, ic, k, 0, i_w);
     }
 }
 
@@ -99,9 +120,9 @@ __global__ void __launch_bounds__(kTrialThreads, 1)
         // phase 1
         if (blk < L.nb_ra) {
             if (blk == 0 && threadIdx.x == 0) bt.act_cnt[(q + 1) & 1] = 0;   // read last in phase 2 of q - 1
-            trial_ra_part<R>(n, bt, q, s0, s1, rc, blk);
+            trial_ra_part<R>(n, bt, q, s0, s1, rc, blk, L.ra_w);
         } else if (blk < L.nb_ra + L.nb_i) {
-            trial_i_part<R>(n, bt, q, s0, s1, ic, blk - L.nb_ra);
+            trial_i_part<R>(n, bt, q, s0, s1, ic, blk - L.nb_ra, L.i_w);
         } else if (q > 0) {
             // the sync closing interval q - 1
             const int k = blk - L.nb_ra - L.nb_i;

@@ -324,11 +324,31 @@ private:
     bool book_dirty_ = false;      // the device bookkeeping changed since the host copy was read
     // the one-launch growth trial (ug_growth_trial.cuh)
     DevMem gTrialCtl_, gActRows_, gSyncEnd_;   // barrier and queue words, row queue, sync steps
+    bool trial_fits_ = false;      // every sync interval fits the trial's segment buffers
+    int trial_key_ = -1;           // the launch mode and role widths trial_blocks_ was sized for
     int trial_blocks_ = 0;         // its grid (0: the network's blocks cannot all be resident)
-    int gloop_trial_launch_ = -1;  // the mode the loop graph was captured with
+    int gloop_trial_launch_ = -1;  // the trial_key_ the loop graph was captured with
+    static int trial_key(const ug::LaunchCtx& lc)
+    {
+        return lc.trial_launch ? 1 + (lc.trial_ra_w << 9 | lc.trial_i_w) : 0;
+    }
+    // Sizes the one-launch trial's grid for the context's launch mode and role widths.
+    ug_status trial_grid(const ug::LaunchCtx& lc)
+    {
+        const int key = trial_key(lc);
+        if (key == trial_key_) return UG_OK;
+        trial_key_ = -1;
+        trial_blocks_ = 0;
+        int ra_w = 0, i_w = 0;
+        if (key && trial_fits_ && ug::trial_widths<R>(lc.trial_ra_w, lc.trial_i_w, &ra_w, &i_w))
+            UG_CUDA(ug::growth_trial_grid<R>(h.n_ra, h.n_i, ra_w, i_w, &trial_blocks_));
+        trial_key_ = key;
+        return UG_OK;
+    }
+    // trial_grid(lc) has sized trial_blocks_ before any use of this
     bool one_launch(const ug::LaunchCtx& lc) const
     {
-        return lc.trial_launch && !lc.timer && trial_blocks_ > 0 && bd_.B == 1 && !bd_.trace_ra && !bd_.trace_i &&
+        return lc.trial_launch && !lc.timer && trial_key_ == trial_key(lc) && trial_blocks_ > 0 && bd_.B == 1 && !bd_.trace_ra && !bd_.trace_i &&
                !bd_.ginh_slot;
     }
     DevMem gTrRaSlot_, gTrISlot_, gTrRaBuf_, gTrIBuf_;   // per-neuron traces
@@ -941,12 +961,13 @@ ug_status NetImpl<R>::growth_init(cudaStream_t st)
     UG_TRY(gActRows_.alloc(4 * (size_t)n * sizeof(int2)));
     UG_TRY(gSyncEnd_.upload(sync_steps, st));
     trial_blocks_ = 0;
+    trial_key_ = -1;
     bool fits = !sync_steps.empty();
     for (size_t q = 0; q < sync_steps.size(); ++q) {
         const int s0 = q == 0 ? 1 : sync_steps[q - 1] + 1;
         if (sync_steps[q] - s0 >= ug::kSegSteps) fits = false;
     }
-    if (fits) UG_CUDA(ug::growth_trial_grid<R>(h.n_ra, h.n_i, &trial_blocks_));
+    trial_fits_ = fits;
     ug::TailDev<R>& t = td_;
     t.n = n;
     t.W = win;
@@ -1048,7 +1069,8 @@ ug_status NetImpl<R>::issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launc
         L.sync_end = gSyncEnd_.as<int>();
         L.Q = Q;
         int nb_sync = 0;
-        ug::trial_roles<R>(h.n_ra, h.n_i, &L.nb_ra, &L.nb_i, &nb_sync);
+        ug::trial_widths<R>(lc.trial_ra_w, lc.trial_i_w, &L.ra_w, &L.i_w);   // checked by trial_grid
+        ug::trial_roles<R>(h.n_ra, h.n_i, L.ra_w, L.i_w, &L.nb_ra, &L.nb_i, &nb_sync);
         L.bar = ctl;
         L.posted = ctl + 1;
         UG_CUDA(ug::launch_growth_trial<R>(gd_, nd_, b, rc_, ic_, L, trial_blocks_, lc.main));
@@ -1083,6 +1105,7 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
     cudaStream_t st = lc.main;
     if (n_trials <= 0) return fail(UG_EINVAL, "n_trials must be positive");
     UG_TRY(prepare_growth_run(training, st));
+    UG_TRY(trial_grid(lc));
     uint32_t trial = first_trial;
     int left = n_trials;
     // kernels per trial: head, the trial (issue_growth_trial), check_bad_values, tail
@@ -1093,7 +1116,7 @@ ug_status NetImpl<R>::run_growth_trials(uint32_t first_trial, int n_trials, int 
         UG_CUDA(cudaMemcpyAsync(gLoop_.as<int>(), words, sizeof(words), cudaMemcpyHostToDevice, st));
         if (graphs && !lc.timer) {
             if (!gloop_ || gloop_training_ != bd_.kick_on || gloop_ginh_gen_ != ginh_gen_ ||
-                gloop_trial_launch_ != lc.trial_launch)
+                gloop_trial_launch_ != trial_key(lc))
                 UG_TRY(capture_growth_loop(lc));
             UG_CUDA(cudaGraphLaunch(gloop_, st));
             UG_CUDA(cudaMemcpyAsync(hloop_, gLoop_.as<int>(), ug::kLoopWords * sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1204,7 +1227,7 @@ ug_status NetImpl<R>::capture_growth_loop(const ug::LaunchCtx& lc)
     UG_CUDA(e);
     gloop_training_ = bd_.kick_on;
     gloop_ginh_gen_ = ginh_gen_;
-    gloop_trial_launch_ = lc.trial_launch;
+    gloop_trial_launch_ = trial_key(lc);
     return UG_OK;
 }
 
@@ -1858,6 +1881,8 @@ struct ug_ctx {
         lc.tail_join = tail_join;
         lc.timer = timer.enabled ? &timer : nullptr;
         lc.trial_launch = trial_launch;
+        lc.trial_ra_w = trial_ra_w;
+        lc.trial_i_w = trial_i_w;
         return lc;
     }
     int64_t launches = 0;
@@ -1867,6 +1892,7 @@ struct ug_ctx {
     int group_ra_bps = 0, group_i_bps = 0;     // integrator blocks per SM of group launches (0: occupancy)
     int group_overlap = 1;                     // interneuron kernel beside the RA kernel
     int trial_launch = 1;                      // growth trials of one network in one cooperative launch
+    int trial_ra_w = 0, trial_i_w = 0;         // its integrating threads per block (0: the default)
     std::recursive_mutex mu;                   // one caller at a time: API calls and the server's rounds
     std::unique_ptr<Server> server;
     ~ug_ctx();
@@ -2348,6 +2374,18 @@ ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch)
     if (!ctx) return fail(UG_EINVAL, "null context");
     std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     ctx->trial_launch = one_launch ? 1 : 0;
+    return UG_OK;
+}
+
+ug_status ug_set_growth_trial_shape(ug_ctx* ctx, int32_t ra_threads, int32_t i_threads)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    for (int w : {ra_threads, i_threads})
+        if (w != 0 && (w < 32 || w > ug::kTrialThreads || w % 32))
+            return fail(UG_EINVAL, "role widths must be 0 or multiples of 32 in [32, 256]");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    ctx->trial_ra_w = ra_threads;
+    ctx->trial_i_w = i_threads;
     return UG_OK;
 }
 

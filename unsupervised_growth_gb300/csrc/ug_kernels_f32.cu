@@ -12,7 +12,7 @@ template cudaError_t launch_growth_epilogue<float>(const GrowthDev&, const Launc
 template cudaError_t launch_growth_remove<float>(const GrowthDev&, const int*, int, cudaStream_t);
 template cudaError_t launch_check_bad<float>(const NetDev<float>&, const BatchDev<float>&, int*, cudaStream_t);
 template cudaError_t epilogue_bulk_grid<float>(int, int, int*);
-template cudaError_t growth_trial_grid<float>(int, int, int*);
+template cudaError_t growth_trial_grid<float>(int, int, int, int, int*);
 template cudaError_t launch_growth_trial<float>(const GrowthDev&, const NetDev<float>&, const BatchDev<float>&,
                                              const RAStep<float>&, const IStep<float>&, const TrialLoop&, int, cudaStream_t);
 template cudaError_t launch_growth_head<float>(const TailDev<float>&, int*, cudaStream_t);

@@ -12,7 +12,7 @@ template cudaError_t launch_growth_epilogue<double>(const GrowthDev&, const Laun
 template cudaError_t launch_growth_remove<double>(const GrowthDev&, const int*, int, cudaStream_t);
 template cudaError_t launch_check_bad<double>(const NetDev<double>&, const BatchDev<double>&, int*, cudaStream_t);
 template cudaError_t epilogue_bulk_grid<double>(int, int, int*);
-template cudaError_t growth_trial_grid<double>(int, int, int*);
+template cudaError_t growth_trial_grid<double>(int, int, int, int, int*);
 template cudaError_t launch_growth_trial<double>(const GrowthDev&, const NetDev<double>&, const BatchDev<double>&,
                                              const RAStep<double>&, const IStep<double>&, const TrialLoop&, int, cudaStream_t);
 template cudaError_t launch_growth_head<double>(const TailDev<double>&, int*, cudaStream_t);

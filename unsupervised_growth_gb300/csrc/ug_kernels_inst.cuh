@@ -175,7 +175,7 @@ cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc)
 constexpr size_t kTrialSmem = (size_t)kTrialWarps * sizeof(RowShared);
 
 template <class R>
-cudaError_t growth_trial_grid(int n_ra, int n_i, int* blocks)
+cudaError_t growth_trial_grid(int n_ra, int n_i, int ra_w, int i_w, int* blocks)
 {
     *blocks = 0;
     cudaError_t e =
@@ -189,7 +189,7 @@ cudaError_t growth_trial_grid(int n_ra, int n_i, int* blocks)
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_growth_trial<R>, kTrialThreads, kTrialSmem);
     if (e != cudaSuccess) return e;
     int nb_ra = 0, nb_i = 0, nb_sync = 0;
-    trial_roles<R>(n_ra, n_i, &nb_ra, &nb_i, &nb_sync);
+    trial_roles<R>(n_ra, n_i, ra_w, i_w, &nb_ra, &nb_i, &nb_sync);
     const long long total = (long long)nb_ra + nb_i + nb_sync;
     if (coop && per_sm > 0 && total <= (long long)per_sm * sms) *blocks = (int)total;
     return cudaSuccess;

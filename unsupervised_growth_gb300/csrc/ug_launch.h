@@ -101,6 +101,8 @@ struct LaunchCtx {
     // growth: the whole trial in one cooperative launch (k_growth_trial) where the
     // network's blocks can all be resident; 0 keeps the per-interval launches
     int trial_launch = 1;
+    // its integrating threads per block of the HVC(RA) and HVC(I) roles (0: the default)
+    int trial_ra_w = 0, trial_i_w = 0;
 };
 
 template <class R>
@@ -130,7 +132,7 @@ cudaError_t launch_growth_epilogue(const GrowthDev& g, const LaunchCtx& lc);
 // The one-launch growth trial (ug_growth_trial.cuh): its grid for a network (0 when the
 // blocks cannot all be resident at once), and the cooperative launch.
 template <class R>
-cudaError_t growth_trial_grid(int n_ra, int n_i, int* blocks);
+cudaError_t growth_trial_grid(int n_ra, int n_i, int ra_w, int i_w, int* blocks);
 template <class R>
 cudaError_t launch_growth_trial(const GrowthDev& g, const NetDev<R>& n, const BatchDev<R>& b, const RAStep<R>& rc,
                                 const IStep<R>& ic, const TrialLoop& L, int blocks, cudaStream_t st);

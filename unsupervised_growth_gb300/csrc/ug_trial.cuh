@@ -444,10 +444,11 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(
 // integrator is a packed f32x2 operation.
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                    const RAStep<R>& rc, int bx, int b)
+                                                    const RAStep<R>& rc, int bx, int b, int width = 0)
 {
     static_assert(sizeof(R) == 4, "the packed RA kernel is single precision");
-    const int t = bx * kBlock + threadIdx.x;
+    // width: neuron pairs of a block (its first `width` threads, whole warps; 0: kBlock)
+    const int t = bx * (width ? width : kBlock) + threadIdx.x;
     const int i0 = 2 * t, i1 = 2 * t + 1;
     const bool v0 = i0 < n.n_ra, v1 = i1 < n.n_ra;
     uint32_t soma0 = 0, dend0 = 0, soma1 = 0, dend1 = 0;
@@ -620,10 +621,11 @@ __global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R
 // events, DP8 in the layout of ug_i_f32.cuh.
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                  const IStep<R>& ic, int bx, int b)
+                                                  const IStep<R>& ic, int bx, int b, int width = 0)
 {
     static_assert(sizeof(R) == 4, "single-precision interneuron kernel");
-    const int i = bx * kBlock + threadIdx.x;
+    // width: interneurons of a block (its first `width` threads, whole warps; 0: kBlock)
+    const int i = bx * (width ? width : kBlock) + threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
