@@ -75,6 +75,24 @@ def test_test_trial_batch_instances_match_solo_runs(engine64, chain_case):
     rn.free()
 
 
+def test_test_trial_batch_instances_match_solo_runs_fp32(engine32, chain_case):
+    """The single build's integrators run one flat grid over (instance, neuron): with 30
+    neuron pairs and 20 interneurons per instance, warps hold neurons of two instances,
+    and each spike must reach its own instance's targets only."""
+    net, _ = chain_case
+    rn = engine32.load_network(net)
+    rn.run_test_trials(0, 5)
+    batch = {k: [_gpu_spikes(rn, k, w) for w in (0, 1, 2)] for k in (1, 4)}
+    st_b = {k: rn.neuron_state(k, 0) for k in (1, 4)}
+    for k in (1, 4):
+        rn.run_test_trials(k, 1)
+        solo = [_gpu_spikes(rn, 0, w) for w in (0, 1, 2)]
+        for a, b in zip(batch[k], solo):
+            assert np.array_equal(a, b), k
+        assert np.array_equal(st_b[k], rn.neuron_state(0, 0)), k
+    rn.free()
+
+
 def test_test_trial_fp32_within_one_step(engine32, chain_case):
     net, ref = chain_case
     rn = engine32.load_network(net)

@@ -93,7 +93,8 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? UG_RA_MIN_BLOCKS : 1)
         act_cnt[2 + ((q + 1) & 1)] = 0; // row kernels of the previous one
     }
     for_items(members, items, *count, M, [&](const GroupMember<R>& m, int bx, int by) {
-        if constexpr (sizeof(R) == 4) interval_ra_x2_body<R, kTrack>(m.n, m.bt, q, s0, s1, m.rc, bx, by);
+        if constexpr (sizeof(R) == 4)
+            interval_ra_x2_body<R, kTrack>(m.n, m.bt, q, s0, s1, m.rc, bx * kBlock + (int)threadIdx.x, by);
         else interval_ra_body<R, kTrack>(m.n, m.bt, q, s0, s1, m.rc, bx, by);
     });
 }
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? UG_I_MIN_BLOCKS : 1)
 {
     __shared__ GroupMember<R> M;
     for_items(members, items, *count, M, [&](const GroupMember<R>& m, int bx, int by) {
-        if constexpr (sizeof(R) == 4) interval_i_x_body(m.n, m.bt, q, s0, s1, m.ic, bx, by);
+        if constexpr (sizeof(R) == 4) interval_i_x_body(m.n, m.bt, q, s0, s1, m.ic, bx * kBlock + (int)threadIdx.x, by);
         else interval_i_body(m.n, m.bt, q, s0, s1, m.ic, bx, by);
     });
 }

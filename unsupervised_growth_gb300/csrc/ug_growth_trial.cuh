@@ -86,7 +86,7 @@ __device__ __forceinline__ void trial_ra_part(const NetDev<R>& n, const BatchDev
 {
     if (threadIdx.x >= ra_w) return;
     if constexpr (sizeof(R) == 4) {
-        interval_ra_x2_body<R>(n, bt, q, s0, s1, rc, k, 0, ra_w);   // pairs [ra_w k, ra_w (k + 1))
+        interval_ra_x2_body<R>(n, bt, q, s0, s1, rc, k * ra_w + (int)threadIdx.x, 0);   // pairs [ra_w k, ra_w (k + 1))
     } else {
         interval_ra_body<R>(n, bt, q, s0, s1, rc, k, 0, ra_w);
     }
@@ -98,7 +98,7 @@ __device__ __forceinline__ void trial_i_part(const NetDev<R>& n, const BatchDev<
 {
     if (threadIdx.x >= i_w) return;
     if constexpr (sizeof(R) == 4) {
-        interval_i_x_body<R>(n, bt, q, s0, s1, ic, k, 0, i_w);      // interneurons [i_w k, i_w (k + 1))
+        interval_i_x_body<R>(n, bt, q, s0, s1, ic, k * i_w + (int)threadIdx.x, 0);   // interneurons [i_w k, i_w (k + 1))
     } else {
         interval_i_body<R>(n, bt, q, s0, s1, ic, k, 0, i_w);
     }

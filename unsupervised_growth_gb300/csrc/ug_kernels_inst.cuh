@@ -49,7 +49,7 @@ inline void launch_i(const NetDev<float>& n, const BatchDev<float>& b, int q, in
                      cudaStream_t st, const LaunchCtx& lc)
 {
     if (lc.timer) lc.timer->begin("k_interval_i", lc.main);
-    const dim3 g((n.n_i + kBlock - 1) / kBlock, b.B);
+    const dim3 g((unsigned)(((long long)b.B * n.n_i + kBlock - 1) / kBlock));   // flat over (instance, interneuron)
     if (b.trace_i)
         k_interval_i_x<float, true><<<g, kBlock, 0, st>>>(n, b, q, s0, s1, ic);
     else
@@ -84,7 +84,7 @@ inline void launch_ra(const NetDev<double>& n, const BatchDev<double>& b, int q,
 inline void launch_ra(const NetDev<float>& n, const BatchDev<float>& b, int q, int s0, int s1, const RAStep<float>& rc,
                       const LaunchCtx& lc)
 {
-    const dim3 g(((n.n_ra + 1) / 2 + kBlock - 1) / kBlock, b.B);
+    const dim3 g((unsigned)(((long long)b.B * ((n.n_ra + 1) / 2) + kBlock - 1) / kBlock));   // flat over (instance, pair)
     if (lc.timer) lc.timer->begin("k_interval_ra", lc.main);
     if (b.ginh_slot || b.trace_ra)
         k_interval_ra_x2<float, true><<<g, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc);

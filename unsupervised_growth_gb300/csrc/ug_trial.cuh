@@ -169,7 +169,8 @@ __device__ __forceinline__ void record_spikes(int* spk_count, int2* spk_buf, int
 // Warp-cooperative scatter of the spikes of every lane: ballot the lanes that
 // spiked, then the whole warp walks each spiker's target list with coalesced
 // loads and adds the fixed-point weight into the ring slot of the sync that
-// will apply it.
+// will apply it.  inst_off is the lane's own instance offset: a warp may hold
+// neurons of two trial instances.
 __device__ __forceinline__ void scatter_warp(uint32_t bits, int src, int s0, const double* T, int num_steps,
                                              const int* syncidx, int ring, const int* off, const int* tgt,
                                              const long long* wq, const double* dly, long long* ring_base,
@@ -181,6 +182,7 @@ __device__ __forceinline__ void scatter_warp(uint32_t bits, int src, int s0, con
         const int sl = __ffs(m) - 1;
         m &= m - 1;
         const int s_src = __shfl_sync(0xffffffffu, src, sl);
+        const size_t s_off = (size_t)__shfl_sync(0xffffffffu, (unsigned long long)inst_off, sl);
         uint32_t b = __shfl_sync(0xffffffffu, bits, sl);
         const int e0 = off[s_src], e1 = off[s_src + 1];
         while (b) {
@@ -191,7 +193,7 @@ __device__ __forceinline__ void scatter_warp(uint32_t bits, int src, int s0, con
                 const int s2 = deliver_step(T, num_steps, s, dly[e]);
                 if (s2 < num_steps) {
                     const size_t slot = (size_t)(syncidx[s2] % ring);
-                    atomicAdd((unsigned long long*)&ring_base[slot * slot_stride + inst_off + tgt[e]],
+                    atomicAdd((unsigned long long*)&ring_base[slot * slot_stride + s_off + tgt[e]],
                               (unsigned long long)wq[e]);
                 }
             }
@@ -444,11 +446,10 @@ __global__ void __launch_bounds__(kBlock, sizeof(R) == 4 ? 8 : 1) k_interval_ra(
 // integrator is a packed f32x2 operation.
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                    const RAStep<R>& rc, int bx, int b, int width = 0)
+                                                    const RAStep<R>& rc, int t, int b)
 {
+    // t: the thread's neuron pair (neurons 2t, 2t + 1; none when 2t >= n_ra), b: its instance
     static_assert(sizeof(R) == 4, "the packed RA kernel is single precision");
-    // width: neuron pairs of a block (its first `width` threads, whole warps; 0: kBlock)
-    const int t = bx * (width ? width : kBlock) + threadIdx.x;
     const int i0 = 2 * t, i1 = 2 * t + 1;
     const bool v0 = i0 < n.n_ra, v1 = i1 < n.n_ra;
     uint32_t soma0 = 0, dend0 = 0, soma1 = 0, dend1 = 0;
@@ -566,7 +567,17 @@ template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(NetDev<R> n, BatchDev<R> bt, int q, int s0,
                                                                            int s1, RAStep<R> rc)
 {
-    interval_ra_x2_body<R, kTrack>(n, bt, q, s0, s1, rc, (int)blockIdx.x, (int)blockIdx.y);
+    // one flat grid over (instance, pair): no block is split between a trial's last
+    // pairs and idle threads
+    // (32-bit: a batch's neuron state outgrows the device long before 2^32 pairs)
+    const unsigned np = (unsigned)(n.n_ra + 1) / 2u;
+    const unsigned g = blockIdx.x * (unsigned)kBlock + threadIdx.x;
+    int b = (int)(g / np), t = (int)(g % np);
+    if (b >= bt.B) {
+        b = bt.B - 1;
+        t = (int)np;   // past the last pair: takes part in the warp's scatter only
+    }
+    interval_ra_x2_body<R, kTrack>(n, bt, q, s0, s1, rc, t, b);
 }
 
 // Single build: draws every Poisson noise event of the trial for each
@@ -621,11 +632,10 @@ __global__ void __launch_bounds__(kBlock) k_noise_events(NetDev<R> n, BatchDev<R
 // events, DP8 in the layout of ug_i_f32.cuh.
 template <class R, bool kTrack = false>
 __device__ __forceinline__ void interval_i_x_body(const NetDev<R>& n, const BatchDev<R>& bt, int q, int s0, int s1,
-                                                  const IStep<R>& ic, int bx, int b, int width = 0)
+                                                  const IStep<R>& ic, int i, int b)
 {
+    // i: the thread's interneuron (none when i >= n_i), b: its instance
     static_assert(sizeof(R) == 4, "single-precision interneuron kernel");
-    // width: interneurons of a block (its first `width` threads, whole warps; 0: kBlock)
-    const int i = bx * (width ? width : kBlock) + threadIdx.x;
     const bool valid = i < n.n_i;
     uint32_t fired_bits = 0;
     if (valid) {
@@ -678,7 +688,14 @@ template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
                                                                          IStep<R> ic)
 {
-    interval_i_x_body<R, kTrack>(n, bt, q, s0, s1, ic, (int)blockIdx.x, (int)blockIdx.y);
+    // one flat grid over (instance, interneuron)
+    const unsigned g = blockIdx.x * (unsigned)kBlock + threadIdx.x;
+    int b = (int)(g / (unsigned)n.n_i), i = (int)(g % (unsigned)n.n_i);
+    if (b >= bt.B) {
+        b = bt.B - 1;
+        i = n.n_i;   // past the last interneuron: takes part in the warp's scatter only
+    }
+    interval_i_x_body<R, kTrack>(n, bt, q, s0, s1, ic, i, b);
 }
 
 // HVC(I) part of one interval; scatters the I->RA kicks of its spikes.
