@@ -42,10 +42,11 @@ SEED = 3
 #   I : 12 stages x 63 ops + 376 ops of the DP8 tableau sums      = 1132 FP32 ops; 12 x (4 ex2 + 1 rcp) = 60 SFU
 FP32_RA, FP32_I = 450, 1132
 MUFU_RA, MUFU_I = 40, 60
-# DRAM bytes per launch of the dominant kernel from an ncu capture of the integrators
-# at 128 trials (16.4 MB read, ~0 written), scaled to a launch of BATCH trials: the state
-# read grows with the trials.
+# DRAM bytes per launch from ncu captures of the integrators at 128 trials (RA 16.4 MB and
+# interneurons 21.8 MB read, ~0 written; the fused launch 38.2 MB), scaled to a launch of
+# BATCH trials: the state read grows with the trials.
 DRAM_BYTES_RA_PER_TRIAL = 16.4e6 / 128
+DRAM_BYTES_I_PER_TRIAL = 21.8e6 / 128
 CPU_WINDOWS = 8   # the headline's CPU baseline advances every core's trial in 8 equal windows
 FP64_BATCH = 64   # test trials per batch of the batched double-precision figure
 SERVE_REQUESTS, SERVE_RATE, SERVE_MAX_TRIALS = 16, 4.0, 10   # the latency leg of the headline
@@ -385,25 +386,31 @@ def run_ours(args, rank, world, local_rank):
         value = trials / (total_ms / 1e3)
         e2e_value = BATCH * args.steps * world / max(sum(e2e_s), 1e-9)
         mufu_peak, fma_peak = calibrate_pipes(local_rank)
-        # per-kernel device time: one more batch with every launch bracketed by events
-        eng.set_kernel_timing(True)
-        rn.run_test_trials(first, BATCH)
-        kt = {k: eng.kernel_timing(k) for k in ("k_interval_ra", "k_interval_i", "k_trial_init")}
-        eng.set_kernel_timing(False)
+        # per-kernel device time: one more batch with every launch bracketed by events, in
+        # the shape the timed steps ran (both integrators of an interval fused in one
+        # launch), then one with the integrators launched apart, for their split
         avg_steps = (NUM_STEPS - 1) / 2000.0   # integration steps per interval launch
-        neuron_steps = {"k_interval_ra": BATCH * N_RA * avg_steps, "k_interval_i": BATCH * N_I * avg_steps}
-        fp32_ops = {"k_interval_ra": FP32_RA, "k_interval_i": FP32_I}
-        sfu_ops = {"k_interval_ra": MUFU_RA, "k_interval_i": MUFU_I}
+        ra_ns, i_ns = BATCH * N_RA * avg_steps, BATCH * N_I * avg_steps
+        work = {"k_interval_x": (ra_ns * FP32_RA + i_ns * FP32_I, ra_ns * MUFU_RA + i_ns * MUFU_I),
+                "k_interval_ra": (ra_ns * FP32_RA, ra_ns * MUFU_RA), "k_interval_i": (i_ns * FP32_I, i_ns * MUFU_I)}
         kernels = {}
-        total_kernel_ms = max(sum(v[0] for v in kt.values()), 1e-9)
-        for k, ns in neuron_steps.items():
-            ms, cnt = kt[k]
-            avg_ms = ms / max(cnt, 1)
-            sec = max(avg_ms, 1e-9) * 1e-3
-            kernels[k] = {"launches": cnt, "avg_launch_ms": avg_ms, "share": ms / total_kernel_ms,
-                          "fp32_ops_per_launch": ns * fp32_ops[k], "fp32_frac": ns * fp32_ops[k] / sec / fma_peak,
-                          "sfu_ops_per_launch": ns * sfu_ops[k], "sfu_frac": ns * sfu_ops[k] / sec / mufu_peak}
-        dom = max(neuron_steps, key=lambda k: kt[k][0])
+        for fused, names in ((True, ("k_interval_x",)), (False, ("k_interval_ra", "k_interval_i"))):
+            eng.set_interval_fusion(fused)
+            eng.set_kernel_timing(True)
+            rn.run_test_trials(first, BATCH)
+            kt = {k: eng.kernel_timing(k) for k in names + ("k_trial_init", "k_noise_events")}
+            eng.set_kernel_timing(False)
+            total_kernel_ms = max(sum(v[0] for v in kt.values()), 1e-9)
+            for k in names:
+                ms, cnt = kt[k]
+                avg_ms = ms / max(cnt, 1)
+                sec = max(avg_ms, 1e-9) * 1e-3
+                ops, sfu = work[k]
+                kernels[k] = {"launches": cnt, "avg_launch_ms": avg_ms, "share": ms / total_kernel_ms,
+                              "fp32_ops_per_launch": ops, "fp32_frac": ops / sec / fma_peak,
+                              "sfu_ops_per_launch": sfu, "sfu_frac": sfu / sec / mufu_peak}
+        eng.set_interval_fusion(True)
+        dom = "k_interval_x"   # the timed steps' kernel: 2001 of their 2003 launches per batch
         per_launch = kernels[dom]["fp32_ops_per_launch"]
         achieved = per_launch / (kernels[dom]["avg_launch_ms"] * 1e-3)
 
@@ -425,8 +432,11 @@ def run_ours(args, rank, world, local_rank):
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved / 1e12, "peak": fma_peak / 1e12, "unit": "T FP32 ops/s",
                          "frac": achieved / fma_peak, "kernel": dom,
-                         "traffic": DRAM_BYTES_RA_PER_TRIAL * BATCH if dom == "k_interval_ra" else None,
-                         "traffic_source": "ncu capture of 128 trials scaled by the trials per launch",
+                         "traffic": (DRAM_BYTES_RA_PER_TRIAL + DRAM_BYTES_I_PER_TRIAL) * BATCH,
+                         "traffic_source": "ncu captures of the integrators at 128 trials, scaled by the trials "
+                                           "per launch",
+                         "split": "k_interval_ra and k_interval_i: the same batch with the integrators launched "
+                                  "apart (ug_set_interval_fusion 0)",
                          "peak_source": "FP32 FMA throughput loop (ug_calibrate_pipes), measured in this run; "
                                         "SFU peak (ex2+rcp loop) also measured",
                          "sfu_peak_gops": mufu_peak / 1e9, "kernels": kernels,

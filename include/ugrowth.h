@@ -170,6 +170,15 @@ ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch);
  * Results are the same bits for every shape; a shape whose blocks cannot all be resident
  * runs the per-interval launches.  UG_EINVAL for other widths. */
 ug_status ug_set_growth_trial_shape(ug_ctx* ctx, int32_t ra_threads, int32_t i_threads);
+/* Launch shape of test batches in the single-precision build, no counterpart in the
+ * reference (whose ranks step every neuron in one loop, NetworkGrowthSimulator.cpp:12820-12835).
+ * fuse 1 (the default): batches of 16 trials or more run the HVC(RA) and HVC(I) integration of
+ * each sync interval in one kernel launch, the interneuron blocks after the RA blocks, so
+ * they fill the SMs the RA part's last wave leaves idle; 0: two launches per interval
+ * (per-kernel timing then reports k_interval_ra and k_interval_i apart; fused, the one
+ * kernel is k_interval_x).  Recording and inhibition tracking always use two launches.
+ * Results are the same bits either way. */
+ug_status ug_set_interval_fusion(ug_ctx* ctx, int32_t fuse);
 /* Serving loop -- no counterpart in the reference.  A scheduler thread of the context
  * runs group rounds (see ug_run_group) over the requests on the GPU and, between
  * rounds, admits queued requests in arrival order while their device footprint fits
@@ -333,7 +342,8 @@ ug_status ug_launch_count(ug_ctx* ctx, int64_t* n);
 /* No counterpart in the reference (measurement support).  While enabled, batches are
  * launched without graphs, one kernel at a time, each bracketed by CUDA events; enabling
  * or disabling clears the totals.  ug_get_kernel_timing returns the summed device time and
- * launch count of one kernel: "k_trial_init", "k_interval_ra" or "k_interval_i". */
+ * launch count of one kernel: "k_trial_init", "k_interval_ra", "k_interval_i" or, for test
+ * batches whose integrators run fused (ug_set_interval_fusion), "k_interval_x". */
 ug_status ug_set_kernel_timing(ug_ctx* ctx, int32_t enabled);
 ug_status ug_get_kernel_timing(ug_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches);
 

@@ -93,6 +93,30 @@ def test_test_trial_batch_instances_match_solo_runs_fp32(engine32, chain_case):
     rn.free()
 
 
+def test_large_batch_fused_integrators_match_solo_runs_fp32(engine32, chain_case):
+    """Batches of 16 trials or more run both integrators of an interval in one launch
+    (k_interval_x: RA blocks first, interneuron blocks after): one kernel per interval
+    instead of two, and each instance gives the bits of the same trial run alone."""
+    net, _ = chain_case
+    rn = engine32.load_network(net)
+    l0 = engine32.launch_count()
+    rn.run_test_trials(0, 3)
+    small = engine32.launch_count() - l0
+    l0 = engine32.launch_count()
+    rn.run_test_trials(0, 20)
+    large = engine32.launch_count() - l0
+    assert large < 0.6 * small, (large, small)
+    batch = {k: [_gpu_spikes(rn, k, w) for w in (0, 1, 2)] for k in (0, 13, 19)}
+    st_b = {k: [rn.neuron_state(k, w) for w in (0, 1)] for k in (0, 13, 19)}
+    for k in (0, 13, 19):
+        rn.run_test_trials(k, 1)
+        for a, b in zip(batch[k], [_gpu_spikes(rn, 0, w) for w in (0, 1, 2)]):
+            assert np.array_equal(a, b), k
+        for w in (0, 1):
+            assert np.array_equal(st_b[k][w], rn.neuron_state(0, w)), (k, w)
+    rn.free()
+
+
 def test_test_trial_fp32_within_one_step(engine32, chain_case):
     net, ref = chain_case
     rn = engine32.load_network(net)

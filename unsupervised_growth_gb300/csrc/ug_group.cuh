@@ -5,8 +5,9 @@
 // launch step all of them through the same interval.
 //
 // Every list kernel runs a fixed, occupancy-sized grid that walks a work list
-// in device memory: item = (member, bx, by), the block coordinates of the
-// single-network launch the item stands for.  The member's descriptors are
+// in device memory: item = (member, bx, by), block bx of the member's trial
+// instance by (kBlock neurons, or neuron pairs in the single build's RA
+// kernel, per block).  The member's descriptors are
 // staged in shared memory when a block moves to another member.  Because the
 // grids and the list addresses are fixed, one captured CUDA graph serves any
 // composition of the group: admitting or retiring a member rewrites the

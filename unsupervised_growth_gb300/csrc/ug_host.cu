@@ -282,6 +282,13 @@ private:
     ug_status ensure_batch(int B);
     ug_status check_error(cudaStream_t st);
     ug_status issue_batch(const ug::LaunchCtx& lc, int64_t* launches);
+    // kernels of one test batch: initialisation (and the noise events), then one launch
+    // per sync interval and integrator, or one per interval when they are fused
+    int64_t batch_launches(const ug::LaunchCtx& lc) const
+    {
+        const int64_t per = ug::fused_interval<R>(nd_, bd_, lc) ? 1 : (h.n_i > 0 ? 2 : 1);
+        return per * ((int64_t)sync_steps.size() + 1) + 1 + (sizeof(R) == 4 && h.n_i > 0 ? 1 : 0);
+    }
     ug_status upload_connectivity(cudaStream_t st);
     ug_status growth_init(cudaStream_t st);
     ug_status issue_growth_trial(const ug::LaunchCtx& lc, int64_t* launches);
@@ -308,6 +315,7 @@ private:
     DevMem ring_ra_exc_, ring_ra_inh_, ring_i_exc_, spk_buf_, spk_count_, error_, trial_, mean_inj_;
     cudaGraphExec_t graph_exec_ = nullptr;
     int graph_B_ = -1;
+    int graph_fuse_ = -1;          // the fusion setting the test-batch graph was captured with
     // growth
     bool growth_ready_ = false;
     bool rara_dirty_ = false;       // device synapse lists changed since the static lists were built
@@ -668,7 +676,7 @@ ug_status NetImpl<R>::issue_batch(const ug::LaunchCtx& lc, int64_t* launches)
     // The last sync (forced at t == num_steps - 1) also raises the conductances
     // (NetworkGrowthSimulator.cpp:9291); an empty interval applies its kicks.
     UG_CUDA(ug::launch_interval<R>(nd_, bd_, Q, h.num_steps, h.num_steps - 1, rc_, ic_, lc));
-    if (launches) *launches += 2 * (Q + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
+    if (launches) *launches += batch_launches(lc);
     return UG_OK;
 }
 
@@ -679,7 +687,7 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
     cudaStream_t st = lc.main;
     UG_TRY(prepare_test(first_trial, n_trials, st));
     if (!graphs || lc.timer) return issue_batch(lc, launches);
-    if (!graph_exec_ || graph_B_ != n_trials) {
+    if (!graph_exec_ || graph_B_ != n_trials || graph_fuse_ != lc.fuse) {
         if (graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
             graph_exec_ = nullptr;
@@ -700,9 +708,10 @@ ug_status NetImpl<R>::run_test_trials(uint32_t first_trial, int n_trials, const 
         cudaGraphDestroy(g);
         UG_CUDA(e);
         graph_B_ = n_trials;
+        graph_fuse_ = lc.fuse;
     }
     UG_CUDA(cudaGraphLaunch(graph_exec_, st));
-    if (launches) *launches += 2 * ((int64_t)sync_steps.size() + 1) + 1 + (sizeof(R) == 4 ? 1 : 0);
+    if (launches) *launches += batch_launches(lc);
     return UG_OK;
 }
 
@@ -1883,6 +1892,7 @@ struct ug_ctx {
         lc.trial_launch = trial_launch;
         lc.trial_ra_w = trial_ra_w;
         lc.trial_i_w = trial_i_w;
+        lc.fuse = interval_fusion;
         return lc;
     }
     int64_t launches = 0;
@@ -1893,6 +1903,7 @@ struct ug_ctx {
     int group_overlap = 1;                     // interneuron kernel beside the RA kernel
     int trial_launch = 1;                      // growth trials of one network in one cooperative launch
     int trial_ra_w = 0, trial_i_w = 0;         // its integrating threads per block (0: the default)
+    int interval_fusion = 1;                   // test batches: both integrators in one launch
     std::recursive_mutex mu;                   // one caller at a time: API calls and the server's rounds
     std::unique_ptr<Server> server;
     ~ug_ctx();
@@ -2374,6 +2385,14 @@ ug_status ug_set_growth_launch(ug_ctx* ctx, int32_t one_launch)
     if (!ctx) return fail(UG_EINVAL, "null context");
     std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
     ctx->trial_launch = one_launch ? 1 : 0;
+    return UG_OK;
+}
+
+ug_status ug_set_interval_fusion(ug_ctx* ctx, int32_t fuse)
+{
+    if (!ctx) return fail(UG_EINVAL, "null context");
+    std::lock_guard<std::recursive_mutex> lk_(ctx->mu);
+    ctx->interval_fusion = fuse ? 1 : 0;
     return UG_OK;
 }
 

@@ -93,10 +93,29 @@ inline void launch_ra(const NetDev<float>& n, const BatchDev<float>& b, int q, i
     if (lc.timer) lc.timer->end(lc.main);
 }
 
+// Both single-build integrators of one interval in one launch (fused_interval).
+inline void launch_fused(const NetDev<double>&, const BatchDev<double>&, int, int, int, const RAStep<double>&,
+                         const IStep<double>&, const LaunchCtx&)
+{
+}
+inline void launch_fused(const NetDev<float>& n, const BatchDev<float>& b, int q, int s0, int s1,
+                         const RAStep<float>& rc, const IStep<float>& ic, const LaunchCtx& lc)
+{
+    const unsigned nb_ra = (unsigned)(((long long)b.B * ((n.n_ra + 1) / 2) + kBlock - 1) / kBlock);
+    const unsigned nb_i = (unsigned)(((long long)b.B * n.n_i + kBlock - 1) / kBlock);
+    if (lc.timer) lc.timer->begin("k_interval_x", lc.main);
+    k_interval_x<float><<<nb_ra + nb_i, kBlock, 0, lc.main>>>(n, b, q, s0, s1, rc, ic, nb_ra);
+    if (lc.timer) lc.timer->end(lc.main);
+}
+
 template <class R>
 cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1, const RAStep<R>& rc,
                             const IStep<R>& ic, const LaunchCtx& lc)
 {
+    if (fused_interval<R>(n, b, lc)) {
+        launch_fused(n, b, q, s0, s1, rc, ic, lc);
+        return cudaGetLastError();
+    }
     // Overlap the two kernels only when a batch is too small to fill the GPU on
     // its own; large batches run them back to back so each SM executes one
     // kernel's code at a time (the integrators do not fit the instruction cache together).

@@ -103,10 +103,22 @@ struct LaunchCtx {
     int trial_launch = 1;
     // its integrating threads per block of the HVC(RA) and HVC(I) roles (0: the default)
     int trial_ra_w = 0, trial_i_w = 0;
+    // test batches: both integrators of an interval in one launch where fused_interval allows
+    int fuse = 1;
 };
 
 template <class R>
 cudaError_t launch_trial_init(const NetDev<R>& n, const BatchDev<R>& b, const LaunchCtx& lc);
+
+// Whether launch_interval runs both integrators in one launch (k_interval_x): the single
+// build's batches of 16 trials or more, without recording or inhibition tracking, unless
+// the context switched fusion off.  Smaller batches overlap the two kernels on two
+// streams instead.
+template <class R>
+inline bool fused_interval(const NetDev<R>& n, const BatchDev<R>& b, const LaunchCtx& lc)
+{
+    return sizeof(R) == 4 && lc.fuse && n.n_i > 0 && b.B >= 16 && !b.trace_ra && !b.trace_i && !b.ginh_slot;
+}
 
 template <class R>
 cudaError_t launch_interval(const NetDev<R>& n, const BatchDev<R>& b, int q, int s0, int s1, const RAStep<R>& rc,

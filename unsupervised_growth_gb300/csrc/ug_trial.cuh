@@ -563,20 +563,27 @@ __device__ __forceinline__ void interval_ra_x2_body(const NetDev<R>& n, const Ba
     }
 }
 
+// Flat grids of the single build's integrators: thread g of a grid over (instance,
+// unit) takes unit g % units of instance g / units, so no block is split between a
+// trial's last units and idle threads.  A thread past the last instance gets the
+// unit index `units` (no neuron) and takes part in its warp's scatter only.
+// (32-bit: a batch's neuron state outgrows the device long before 2^32 units.)
+__device__ __forceinline__ void flat_unit(unsigned g, unsigned units, int B, int& u, int& b)
+{
+    b = (int)(g / units);
+    u = (int)(g % units);
+    if (b >= B) {
+        b = B - 1;
+        u = (int)units;
+    }
+}
+
 template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_ra_x2(NetDev<R> n, BatchDev<R> bt, int q, int s0,
                                                                            int s1, RAStep<R> rc)
 {
-    // one flat grid over (instance, pair): no block is split between a trial's last
-    // pairs and idle threads
-    // (32-bit: a batch's neuron state outgrows the device long before 2^32 pairs)
-    const unsigned np = (unsigned)(n.n_ra + 1) / 2u;
-    const unsigned g = blockIdx.x * (unsigned)kBlock + threadIdx.x;
-    int b = (int)(g / np), t = (int)(g % np);
-    if (b >= bt.B) {
-        b = bt.B - 1;
-        t = (int)np;   // past the last pair: takes part in the warp's scatter only
-    }
+    int t, b;   // one flat grid over (instance, neuron pair)
+    flat_unit(blockIdx.x * (unsigned)kBlock + threadIdx.x, (unsigned)(n.n_ra + 1) / 2u, bt.B, t, b);
     interval_ra_x2_body<R, kTrack>(n, bt, q, s0, s1, rc, t, b);
 }
 
@@ -688,14 +695,29 @@ template <class R, bool kTrack = false>
 __global__ void __launch_bounds__(kBlock, UG_I_MIN_BLOCKS) k_interval_i_x(NetDev<R> n, BatchDev<R> bt, int q, int s0, int s1,
                                                                          IStep<R> ic)
 {
-    // one flat grid over (instance, interneuron)
-    const unsigned g = blockIdx.x * (unsigned)kBlock + threadIdx.x;
-    int b = (int)(g / (unsigned)n.n_i), i = (int)(g % (unsigned)n.n_i);
-    if (b >= bt.B) {
-        b = bt.B - 1;
-        i = n.n_i;   // past the last interneuron: takes part in the warp's scatter only
-    }
+    int i, b;   // one flat grid over (instance, interneuron)
+    flat_unit(blockIdx.x * (unsigned)kBlock + threadIdx.x, (unsigned)n.n_i, bt.B, i, b);
     interval_i_x_body<R, kTrack>(n, bt, q, s0, s1, ic, i, b);
+}
+
+// Single build, large batches: both integrators of one interval in one launch.  Blocks
+// [0, nb_ra) take the flat grid of HVC(RA) neuron pairs, the rest the flat grid of
+// interneurons.  The two parts read and clear the ring slots of the previous sync and
+// add only into slots of this sync or later, as when they run on two streams, so any
+// block of either part may run beside any other.  One launch lets interneuron blocks
+// fill the SMs that the RA part's last partial wave leaves idle.
+template <class R>
+__global__ void __launch_bounds__(kBlock, UG_RA_MIN_BLOCKS) k_interval_x(NetDev<R> n, BatchDev<R> bt, int q, int s0,
+                                                                       int s1, RAStep<R> rc, IStep<R> ic, unsigned nb_ra)
+{
+    int u, b;
+    if (blockIdx.x < nb_ra) {
+        flat_unit(blockIdx.x * (unsigned)kBlock + threadIdx.x, (unsigned)(n.n_ra + 1) / 2u, bt.B, u, b);
+        interval_ra_x2_body<R>(n, bt, q, s0, s1, rc, u, b);
+    } else {
+        flat_unit((blockIdx.x - nb_ra) * (unsigned)kBlock + threadIdx.x, (unsigned)n.n_i, bt.B, u, b);
+        interval_i_x_body<R>(n, bt, q, s0, s1, ic, u, b);
+    }
 }
 
 // HVC(I) part of one interval; scatters the I->RA kicks of its spikes.

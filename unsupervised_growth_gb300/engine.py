@@ -24,7 +24,7 @@ UG_STATUS = {0: "UG_OK", 1: "UG_EINVAL", 2: "UG_ENOMEM", 3: "UG_EIO", 4: "UG_ENU
 # Every entry point of include/ugrowth.h, in declaration order.
 EXPORTED = ["ug_last_error", "ug_create", "ug_destroy", "ug_set_stream", "ug_synchronize", "ug_load_network",
             "ug_free_network", "ug_run_test_trials", "ug_run_growth_trials", "ug_run_group", "ug_set_group_launch",
-            "ug_set_growth_launch", "ug_set_growth_trial_shape", "ug_server_start", "ug_submit", "ug_poll", "ug_server_stop", "ug_get_weights", "ug_get_delays",
+            "ug_set_growth_launch", "ug_set_growth_trial_shape", "ug_set_interval_fusion", "ug_server_start", "ug_submit", "ug_poll", "ug_server_stop", "ug_get_weights", "ug_get_delays",
             "ug_get_synapse_list", "ug_get_neuron_props", "ug_get_replaced", "ug_get_connections",
             "ug_get_coordinates", "ug_get_connection_lengths", "ug_get_network_info", "ug_get_activity_history",
             "ug_get_training", "ug_load_network_dir", "ug_write_state_dir", "ug_write_topology_dir",
@@ -179,6 +179,7 @@ def load_library(path: str = LIB_PATH):
     L.ug_set_group_launch.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32]
     L.ug_set_growth_launch.argtypes = [vp, C.c_int32]
     L.ug_set_growth_trial_shape.argtypes = [vp, C.c_int32, C.c_int32]
+    L.ug_set_interval_fusion.argtypes = [vp, C.c_int32]
     L.ug_server_start.argtypes = [vp, C.POINTER(ServerOpts)]
     L.ug_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
     L.ug_poll.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(RequestInfo)]
@@ -480,6 +481,11 @@ class Engine:
         """Single-network growth trials in one cooperative launch each (default), or in
         per-interval launches; the results are the same bits."""
         _check(self.L.ug_set_growth_launch(self.ctx, 1 if one_launch else 0))
+
+    def set_interval_fusion(self, fuse: bool = True):
+        """Test batches of 16 trials or more: both integrators of an interval in one launch
+        (default) or two; the results are the same bits."""
+        _check(self.L.ug_set_interval_fusion(self.ctx, 1 if fuse else 0))
 
     def set_growth_trial_shape(self, ra_threads: int = 0, i_threads: int = 0):
         """Integrating threads per block of the HVC(RA) and HVC(I) roles of the one-launch
