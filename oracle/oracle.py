@@ -459,8 +459,8 @@ class RefSimNet(OracleNet):
     """The same network held by the reference's own simulator class
     (NetworkGrowthSimulator, compiled from the reference tree into _ref/), driven
     through the harness in ref_harness/sim_harness.cpp.  Same methods as
-    OracleNet except the trace, delivery-log and inhibition hooks, which exist
-    only in the restatement."""
+    OracleNet except the trace and delivery-log hooks, which exist only in the
+    restatement; inhibition tracking runs the reference's own tracking trial."""
 
     def __init__(self, net, opt: str = "O2"):
         R = ref_sim_lib(opt)

@@ -19,6 +19,11 @@
  *    per-trial tail of chain_growth (:5841-5875): trial counters,
  *    check_neuron_activity, update_neuron_properties_sameDendrite_diffMaturationRate,
  *    replace_neurons;
+ *  - with inhibition tracking set, the growth trial is
+ *    trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking
+ *    (:8085-8838) into Ginh_local, sized by the reference's
+ *    initialize_local_inhibitory_conductances (:16172-16178), as
+ *    chain_growth_with_inhibition_tracking loops (:5662-5760);
  *  - a test trial: reset_after_chain_test (:4553-4589) then
  *    trial_no_stdp_fixedSpread (:12747-13117), as test_chain loops (:1395-1470);
  *  - noise: before each trial every neuron's generator is re-pointed (the
@@ -78,6 +83,25 @@ public:
     std::vector<double> spread;
     std::vector<int> replaced;
     std::unordered_map<uint64_t, int> step_of_time;
+    double ginh_res = 0.0;    /* inhibition-tracking resolution in ms; 0: the plain growth trial */
+
+    void set_inhibition_tracking(double resolution)
+    {
+        ensure_initialized();
+        ginh_res = resolution > 0 ? resolution : 0.0;
+        if (ginh_res > 0) initialize_local_inhibitory_conductances(ginh_res);
+    }
+
+    /* The last tracked trial's record in neuron-id order, [n_ra][points]; returns points. */
+    int32_t inhibition(double* out, int64_t capacity) const
+    {
+        if (ginh_res <= 0 || Ginh_local.empty()) return 0;
+        const int32_t points = (int32_t)Ginh_local[0].size();
+        if (out && capacity >= (int64_t)N_RA * points)
+            for (int i = 0; i < N_RA_local; ++i)
+                std::copy(Ginh_local[i].begin(), Ginh_local[i].end(), out + (size_t)Id_RA_local[i] * points);
+        return points;
+    }
 
     void set_params(const ugo_synaptic_params* syn, const ugo_maturation_params* mat, const ugo_noise_params* noise,
                     const ugo_connection_params* conn)
@@ -192,7 +216,10 @@ public:
         } else {
             setToRest_afterEpoch();
             noise_generator.bind(seed, UGO_KIND_TRIAL, net_id, 0, trial);
-            trial_1stSoma_pre_1stSoma_post_delays_fixedSpread(training, spread);
+            if (ginh_res > 0)
+                trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking(training, spread, ginh_res);
+            else
+                trial_1stSoma_pre_1stSoma_post_delays_fixedSpread(training, spread);
         }
         return check_bad_values() < 0 ? -1 : 0;
     }
@@ -460,6 +487,9 @@ int32_t refsim_run_trial(void* h, int32_t kind, int32_t training, uint32_t trial
 }
 
 int32_t refsim_after_growth_trial(void* h, uint32_t trial) { return S(h)->after_growth_trial(trial); }
+
+void refsim_set_inhibition_tracking(void* h, double resolution) { S(h)->set_inhibition_tracking(resolution); }
+int32_t refsim_get_inhibition(void* h, double* out, int64_t capacity) { return S(h)->inhibition(out, capacity); }
 
 int64_t refsim_get_spikes(void* h, int32_t which, int32_t* neuron, int32_t* step, int64_t cap)
 {

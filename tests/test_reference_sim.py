@@ -15,7 +15,8 @@ with their per-trial tail (trial_1stSoma_pre_1stSoma_post_delays_fixedSpread,
 form and rows saturate and remodel, replacement of silent neurons (:15757-15881,
 :157-220, :528-618), the 300/100 growth network with the STDP parameters of the
 config-1 workload (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold 0.035,
-Nss 3), a state directory read by the reference's own read_network_state
+Nss 3), the growth variant with inhibition tracking (:8085-8838: its Ginh_d
+record too), a state directory read by the reference's own read_network_state
 (:1943-2020) through its libconfig readers, and the reference built with its
 shipped flags (-g, no optimisation) against the -O2 build.
 
@@ -84,6 +85,30 @@ def test_growth_trials_match_reference():
         assert_same_state(o, r, t)
     assert sum(map(len, o.synapse_list(1))) > 0             # supersynapses formed
     assert o.neuron_props()["remodeled"].sum() > 0          # saturated rows were remodeled
+
+
+@pytest.mark.parametrize("res", [0.37, 1.0])
+def test_inhibition_tracking_matches_reference(res):
+    """The growth variant with inhibition tracking: the oracle's tracking flag on its growth
+    trial against the reference's own separate trial function,
+    trial_1stSoma_pre_1stSoma_post_delays_fixedSpread_with_inhibition_tracking (:8085-8838).
+    Spikes, weights, lists and the Ginh_d record are the same bits; 0.37 ms is not a
+    multiple of the 0.25 ms synchronisation period, so records fall both on and between
+    synchronising steps."""
+    net = growth_net()
+    o, r = OracleNet(net), RefSimNet(net)
+    o.set_inhibition_tracking(res)
+    r.set_inhibition_tracking(res)
+    for t in range(3):
+        assert o.run_trial(True, t) == 0
+        assert r.run_trial(True, t) == 0
+        assert o.after_growth_trial(t) == r.after_growth_trial(t) == 0
+        assert_same_state(o, r, t)
+        ro, rr = o.inhibition(), r.inhibition()
+        assert ro.shape == rr.shape == (net.n_ra, int(500.0 / res)), (ro.shape, rr.shape)
+        assert np.array_equal(ro, rr), t
+        assert rr.max() > 0
+    assert sum(map(len, o.synapse_list(1))) > 0             # supersynapses formed
 
 
 def test_replacement_matches_reference():
