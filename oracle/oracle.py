@@ -470,6 +470,17 @@ class RefSimNet(OracleNet):
         if R.refsim_set_num_steps(self.h, int(net.num_steps)) != 0:
             raise ValueError("the reference's trial is 25000 steps; the network asks for %d" % net.num_steps)
 
+    def set_recording(self, ra_ids, i_ids, trial: int, directory: str):
+        """The reference's set_recording (NetworkGrowthSimulator.cpp:2352-2407): the listed
+        neurons write their state before every step of the next trial into
+        directory/RA/RA<id>_trial<trial>.bin and directory/I/I<id>_trial<trial>.bin."""
+        ra = np.ascontiguousarray(ra_ids, dtype=np.int32)
+        ii = np.ascontiguousarray(i_ids, dtype=np.int32)
+        f = self.L.ugo_set_recording
+        f.argtypes = [C.c_void_p, _i32p, C.c_int32, _i32p, C.c_int32, C.c_int32, C.c_char_p]
+        f(self.h, _ptr(ra, _i32p), len(ra), _ptr(ii, _i32p), len(ii), int(trial),
+          (os.path.join(directory, "")).encode())
+
     @classmethod
     def from_dir(cls, directory: str, trial: int, seed: int, net_id: int = 0, opt: str = "O2"):
         """A network read by the reference's own read_network_state from a state

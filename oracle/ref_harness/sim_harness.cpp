@@ -26,6 +26,9 @@
  *    chain_growth_with_inhibition_tracking loops (:5662-5760);
  *  - a test trial: reset_after_chain_test (:4553-4589) then
  *    trial_no_stdp_fixedSpread (:12747-13117), as test_chain loops (:1395-1470);
+ *  - per-neuron traces: the reference's own set_recording (:2352-2407), called
+ *    before a trial as test_chain calls it (:1402), so the neuron classes write
+ *    their RA<id>_trial<k>.bin / I<id>_trial<k>.bin files;
  *  - noise: before each trial every neuron's generator is re-pointed (the
  *    reference's set_noise_generator, HH2_test.h:74, HHI_buffer.h:46) to its
  *    own counter-based stream, and the simulator's own generator to the trial's
@@ -90,6 +93,15 @@ public:
         ensure_initialized();
         ginh_res = resolution > 0 ? resolution : 0.0;
         if (ginh_res > 0) initialize_local_inhibitory_conductances(ginh_res);
+    }
+
+    /* The reference's set_recording: the listed neurons write their state before every step
+     * of the next trials into dir/RA/ and dir/I/ (dir ends with '/'). */
+    void record(const std::vector<int>& ra, const std::vector<int>& in, int trial, const char* dir)
+    {
+        ensure_initialized();
+        Quiet q(own_stdout);
+        set_recording(ra, in, trial, dir);
     }
 
     /* The last tracked trial's record in neuron-id order, [n_ra][points]; returns points. */
@@ -489,6 +501,12 @@ int32_t refsim_run_trial(void* h, int32_t kind, int32_t training, uint32_t trial
 int32_t refsim_after_growth_trial(void* h, uint32_t trial) { return S(h)->after_growth_trial(trial); }
 
 void refsim_set_inhibition_tracking(void* h, double resolution) { S(h)->set_inhibition_tracking(resolution); }
+
+void refsim_set_recording(void* h, const int32_t* ra, int32_t n_ra, const int32_t* in, int32_t n_i, int32_t trial,
+                          const char* dir)
+{
+    S(h)->record(std::vector<int>(ra, ra + n_ra), std::vector<int>(in, in + n_i), trial, dir);
+}
 int32_t refsim_get_inhibition(void* h, double* out, int64_t capacity) { return S(h)->inhibition(out, capacity); }
 
 int64_t refsim_get_spikes(void* h, int32_t which, int32_t* neuron, int32_t* step, int64_t cap)

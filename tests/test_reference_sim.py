@@ -16,7 +16,8 @@ form and rows saturate and remodel, replacement of silent neurons (:15757-15881,
 :157-220, :528-618), the 300/100 growth network with the STDP parameters of the
 config-1 workload (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold 0.035,
 Nss 3), the growth variant with inhibition tracking (:8085-8838: its Ginh_d
-record too), a state directory read by the reference's own read_network_state
+record too), the trace files of the reference's own set_recording (:2352-2407),
+a state directory read by the reference's own read_network_state
 (:1943-2020) through its libconfig readers, and the reference built with its
 shipped flags (-g, no optimisation) against the -O2 build.
 
@@ -109,6 +110,44 @@ def test_inhibition_tracking_matches_reference(res):
         assert np.array_equal(ro, rr), t
         assert rr.max() > 0
     assert sum(map(len, o.synapse_list(1))) > 0             # supersynapses formed
+
+
+def test_traces_match_reference_files(tmp_path):
+    """Per-neuron traces: the reference's own set_recording (:2352-2407), called before a
+    test trial as test_chain does (:1402), makes HH2_test / HHI_buffer write the state
+    before every step in whole 1000-record buffers (HH2_test.cpp:394-411, 476-497;
+    HHI_buffer.cpp:148-167).  Those files equal the oracle's per-step traces bit for bit:
+    the record before step s is the oracle's state after step s - 1."""
+    net = small_chain(seed=5)
+    train = set(np.asarray(net.training).tolist())
+    ra = [i for i in range(net.n_ra) if i not in train][::7][:4]
+    ii = [0, 7, 13]
+    o = OracleNet(net)
+    o.set_trace(ra_ids=ra, i_ids=ii)
+    assert o.run_trial(False, 3) == 0
+    tra, tri = o.trace()                      # [steps + 1][k][10], [steps + 1][k][7]
+    (tmp_path / "RA").mkdir()
+    (tmp_path / "I").mkdir()
+    r = RefSimNet(net)
+    r.set_recording(ra, ii, 3, str(tmp_path))
+    assert r.run_trial(False, 3) == 0
+    rows = (net.num_steps - 1) // 1000 * 1000  # the last partial buffer is never written
+    T = np.zeros(rows)                         # the neurons' time: t += 0.02 per step
+    t = 0.0
+    for s in range(1, rows):
+        t += 0.02
+        T[s] = t
+    for k, i in enumerate(ra):
+        raw = np.fromfile(tmp_path / "RA" / f"RA{i}_trial3.bin", dtype=np.float64).reshape(-1, 5)
+        assert raw.shape == (rows, 5)
+        assert np.array_equal(raw[:, 0], T), i
+        assert np.array_equal(raw[:, 1:], tra[:rows, k][:, [0, 1, 8, 9]]), i   # Vs, Vd, Gexc_d, Ginh_d
+    for k, i in enumerate(ii):
+        raw = np.fromfile(tmp_path / "I" / f"I{i}_trial3.bin", dtype=np.float64).reshape(-1, 4)
+        assert raw.shape == (rows, 4)
+        assert np.array_equal(raw[:, 0], T), i
+        assert np.array_equal(raw[:, 1:], tri[:rows, k][:, [0, 5, 6]]), i      # V, Gexc, Ginh
+    assert tra[:, :, 0].max() > 0             # the recorded neurons spiked
 
 
 def test_replacement_matches_reference():
