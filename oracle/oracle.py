@@ -263,6 +263,41 @@ def generate_topology(params: dict, n_ra: int, n_i: int, n_tr: int, seed: int, n
                 ra_attempts=counters[0], i_retries=counters[1])
 
 
+def reference_topology(params: dict, n_ra: int, n_i: int, seed: int, net: int = 0, opt: str = "O2") -> dict:
+    """createNetworkForGrowth's sampling on the sphere in the reference's own code
+    (NetworkGrowthSimulator::sample_coordinates and sample_connections, run by the harness
+    in ref_harness/sim_harness.cpp on a topology stream): coordinates, the model
+    interneuron distance and the RA->I / I->RA lists with their lengths, in the layout of
+    generate_topology."""
+    R = ref_sim_lib(opt)
+    if R is None:
+        raise RuntimeError("the reference simulator is not built (oracle/Makefile target refsim)")
+    R.refsim_new.restype = C.c_void_p
+    R.refsim_new.argtypes = [C.c_int32, C.c_int32]
+    R.refsim_free.argtypes = [C.c_void_p]
+    R.refsim_topology.argtypes = [C.c_void_p] + [C.c_double] * 4 + [C.c_uint64, C.c_uint32]
+    R.refsim_topology_connections.restype = C.c_int64
+    R.refsim_topology_connections.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _f64p]
+    R.refsim_topology_model_distance.restype = C.c_double
+    R.refsim_topology_model_distance.argtypes = [C.c_void_p]
+    R.refsim_get_coordinates.argtypes = [C.c_void_p, _f64p, _f64p]
+    h = R.refsim_new(n_ra, n_i)
+    try:
+        R.refsim_topology(h, *(float(params[k]) for k in ("A_RA2I", "SIGMA_RA2I", "B_I2RA", "SIGMA_I2RA")),
+                          int(seed), int(net))
+        ra, ii = np.zeros((n_ra, 3)), np.zeros((n_i, 3))
+        R.refsim_get_coordinates(h, _ptr(ra, _f64p), _ptr(ii, _f64p))
+        lists = []
+        for which, n_src in ((0, n_ra), (1, n_i)):
+            n = R.refsim_topology_connections(h, which, None, None, None)
+            off, tgt, ln = np.zeros(n_src + 1, dtype=np.int32), np.zeros(max(n, 1), dtype=np.int32), np.zeros(max(n, 1))
+            R.refsim_topology_connections(h, which, _ptr(off, _i32p), _ptr(tgt, _i32p), _ptr(ln, _f64p))
+            lists.append((off, tgt[:n], ln[:n]))
+        return dict(ra_xyz=ra, i_xyz=ii, model=R.refsim_topology_model_distance(h), ri=lists[0], ir=lists[1])
+    finally:
+        R.refsim_free(h)
+
+
 def _kicks(kicks):
     kicks = sorted(kicks or [])
     steps = np.array([k[0] for k in kicks], dtype=np.int32)

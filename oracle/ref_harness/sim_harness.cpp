@@ -26,6 +26,10 @@
  *    chain_growth_with_inhibition_tracking loops (:5662-5760);
  *  - a test trial: reset_after_chain_test (:4553-4589) then
  *    trial_no_stdp_fixedSpread (:12747-13117), as test_chain loops (:1395-1470);
+ *  - topology: createNetworkForGrowth's sampling in the reference's own code,
+ *    generate_network_topology (:110-155) without its file writers:
+ *    sample_coordinates (:222-457) and sample_connections (:620-700) on the
+ *    sphere, drawing from the simulator's generator bound to a topology stream;
  *  - per-neuron traces: the reference's own set_recording (:2352-2407), called
  *    before a trial as test_chain calls it (:1402), so the neuron classes write
  *    their RA<id>_trial<k>.bin / I<id>_trial<k>.bin files;
@@ -94,6 +98,55 @@ public:
         ginh_res = resolution > 0 ? resolution : 0.0;
         if (ginh_res > 0) initialize_local_inhibitory_conductances(ginh_res);
     }
+
+    /* The reference's topology sampling on the sphere (generate_network_topology's arrays,
+     * then sample_coordinates and sample_connections); the weights and delays it also
+     * draws are not compared. */
+    void topology(double a_ra2i, double s_ra2i, double b_i2ra, double s_i2ra, uint64_t s, uint32_t net)
+    {
+        Quiet q(own_stdout);
+        topology_params.arrangement = "sphere";
+        topology_params.A_RA2I = a_ra2i;
+        topology_params.SIGMA_RA2I = s_ra2i;
+        topology_params.B_I2RA = b_i2ra;
+        topology_params.SIGMA_I2RA = s_i2ra;
+        connection_params.Gei_max = 1.0;
+        connection_params.Gie_max = 1.0;
+        connection_params.delay_constant = 0.0;
+        for (vector<double>* v : {&xx_RA, &yy_RA, &zz_RA}) v->assign(N_RA, 0.0);
+        for (vector<double>* v : {&xx_I, &yy_I, &zz_I}) v->assign(N_I, 0.0);
+        training_neurons.assign(N_TR, 0);
+        weights_RA_I_global.assign(N_RA, {});
+        syn_ID_RA_I_global.assign(N_RA, {});
+        syn_lengths_RA_I_global.assign(N_RA, {});
+        axonal_delays_RA_I_global.assign(N_RA, {});
+        weights_I_RA_global.assign(N_I, {});
+        syn_ID_I_RA_global.assign(N_I, {});
+        syn_lengths_I_RA_global.assign(N_I, {});
+        axonal_delays_I_RA_global.assign(N_I, {});
+        noise_generator.bind(s, UGO_KIND_TOPOLOGY, net, 0, 0);
+        sample_coordinates();
+        sample_connections();
+    }
+
+    /* The sampled lists: which 0 RA->I, 1 I->RA, as CSR with the pair distances. */
+    int64_t topology_connections(int which, int32_t* off, int32_t* tgt, double* len) const
+    {
+        const vector<vector<int>>& ids = which == 0 ? syn_ID_RA_I_global : syn_ID_I_RA_global;
+        const vector<vector<double>>& ls = which == 0 ? syn_lengths_RA_I_global : syn_lengths_I_RA_global;
+        int64_t n = 0;
+        for (size_t i = 0; i < ids.size(); ++i) {
+            if (off) off[i] = (int32_t)n;
+            for (size_t k = 0; k < ids[i].size(); ++k, ++n) {
+                if (tgt) tgt[n] = ids[i][k];
+                if (len) len[n] = ls[i][k];
+            }
+        }
+        if (off) off[ids.size()] = (int32_t)n;
+        return n;
+    }
+
+    double model_distance() const { return MODEL_INTERNEURON_DISTANCE; }
 
     /* The reference's set_recording: the listed neurons write their state before every step
      * of the next trials into dir/RA/ and dir/I/ (dir ends with '/'). */
@@ -501,6 +554,17 @@ int32_t refsim_run_trial(void* h, int32_t kind, int32_t training, uint32_t trial
 int32_t refsim_after_growth_trial(void* h, uint32_t trial) { return S(h)->after_growth_trial(trial); }
 
 void refsim_set_inhibition_tracking(void* h, double resolution) { S(h)->set_inhibition_tracking(resolution); }
+
+void refsim_topology(void* h, double a_ra2i, double s_ra2i, double b_i2ra, double s_i2ra, uint64_t seed,
+                     uint32_t net)
+{
+    S(h)->topology(a_ra2i, s_ra2i, b_i2ra, s_i2ra, seed, net);
+}
+int64_t refsim_topology_connections(void* h, int32_t which, int32_t* off, int32_t* tgt, double* len)
+{
+    return S(h)->topology_connections(which, off, tgt, len);
+}
+double refsim_topology_model_distance(void* h) { return S(h)->model_distance(); }
 
 void refsim_set_recording(void* h, const int32_t* ra, int32_t n_ra, const int32_t* in, int32_t n_i, int32_t trial,
                           const char* dir)

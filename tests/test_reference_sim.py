@@ -16,7 +16,8 @@ form and rows saturate and remodel, replacement of silent neurons (:15757-15881,
 :157-220, :528-618), the 300/100 growth network with the STDP parameters of the
 config-1 workload (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold 0.035,
 Nss 3), the growth variant with inhibition tracking (:8085-8838: its Ginh_d
-record too), the trace files of the reference's own set_recording (:2352-2407),
+record too), the trace files of the reference's own set_recording (:2352-2407), the
+distribution of networks from the reference's own topology sampling (:222-700),
 a state directory read by the reference's own read_network_state
 (:1943-2020) through its libconfig readers, and the reference built with its
 shipped flags (-g, no optimisation) against the -O2 build.
@@ -148,6 +149,53 @@ def test_traces_match_reference_files(tmp_path):
         assert np.array_equal(raw[:, 0], T), i
         assert np.array_equal(raw[:, 1:], tri[:rows, k][:, [0, 5, 6]]), i      # V, Gexc, Ginh
     assert tra[:, :, 0].max() > 0             # the recorded neurons spiked
+
+
+def _ks(a, b):
+    """Two-sample Kolmogorov-Smirnov statistic."""
+    a, b = np.sort(a), np.sort(b)
+    x = np.concatenate([a, b])
+    return np.abs(np.searchsorted(a, x, side="right") / len(a) - np.searchsorted(b, x, side="right") / len(b)).max()
+
+
+def _nearest(xyz, model):
+    """Each neuron's nearest-neighbour arc distance on the unit sphere, in microns."""
+    G = np.clip(xyz @ xyz.T, -1.0, 1.0)
+    np.fill_diagonal(G, -1.0)
+    return np.arccos(G.max(axis=1)) * 40.0 / model
+
+
+def test_topology_distribution_matches_reference():
+    """createNetworkForGrowth at its sizes (2000 HVC(RA), 550 HVC(I) on the sphere): the
+    oracle's restatement of the device sampler against the reference's own
+    sample_coordinates and sample_connections (:222-457, :620-700).  They consume their
+    random numbers in different orders (the device filters batches of attempts), so the
+    comparison is distributional, pooled over four networks each: the model interneuron
+    distance, the connection counts within 5 sigma, the connection lengths and the
+    nearest-neighbour distances by two-sample Kolmogorov-Smirnov statistics, the spread of
+    out-degrees, and the minimum intersomatic distance."""
+    P = dict(A_RA2I=0.1, SIGMA_RA2I=120 / np.sqrt(2.0), B_I2RA=0.1, SIGMA_I2RA=120 / np.sqrt(2.0))
+    ref = [O.reference_topology(P, 2000, 550, seed=s) for s in range(4)]
+    orc = [O.generate_topology(P, 2000, 550, 10, seed=100 + s) for s in range(4)]
+    model = ref[0]["model"]
+    assert all(t["model"] == model for t in ref + orc)
+    for key in ("ri", "ir"):
+        nr = np.array([len(t[key][1]) for t in ref], dtype=float)
+        no = np.array([len(t[key][1]) for t in orc], dtype=float)
+        assert abs(nr.mean() - no.mean()) < 5 * np.sqrt((nr.mean() + no.mean()) / 4), (key, nr, no)
+        lr = np.concatenate([t[key][2] for t in ref])
+        lo = np.concatenate([t[key][2] for t in orc])
+        assert _ks(lr, lo) < 0.025, (key, _ks(lr, lo))
+        dr = np.concatenate([np.diff(t[key][0]) for t in ref])
+        do = np.concatenate([np.diff(t[key][0]) for t in orc])
+        assert abs(dr.std() / do.std() - 1) < 0.1, (key, dr.std(), do.std())
+    for part, lim in (("ra_xyz", 0.04), ("i_xyz", 0.07)):
+        nr = np.concatenate([_nearest(t[part], model) for t in ref])
+        no = np.concatenate([_nearest(t[part], model) for t in orc])
+        assert _ks(nr, no) < lim, (part, _ks(nr, no))
+    for t in ref + orc:
+        pts = np.vstack([t["i_xyz"], t["ra_xyz"]])
+        assert _nearest(pts, model).min() >= 10.0 - 1e-9   # MIN_INTERSOMATIC_DISTANCE, microns
 
 
 def test_replacement_matches_reference():
