@@ -13,7 +13,7 @@ Covered: test trials (trial_no_stdp_fixedSpread, :12747-13117), growth trials
 with their per-trial tail (trial_1stSoma_pre_1stSoma_post_delays_fixedSpread,
 :8839-9571; chain_growth :5841-5875) on the fast-growth set where supersynapses
 form and rows saturate and remodel, replacement of silent neurons (:15757-15881,
-:157-220, :528-618), the 300/100 growth network with the STDP parameters of the
+:157-220, :528-618), also staggered over twenty consecutive trials, the 300/100 growth network with the STDP parameters of the
 config-1 workload (tau 30 ms, A_P = 1.05 A_D, supersynapse threshold 0.035,
 Nss 3), the growth variant with inhibition tracking (:8085-8838: its Ginh_d
 record too), the trace files of the reference's own set_recording (:2352-2407), the
@@ -216,6 +216,39 @@ def test_replacement_matches_reference():
             assert np.array_equal(x, y), t
         if t == 0:
             assert sorted(o.replaced().tolist()) == sorted(silent)
+
+
+def test_long_growth_run_with_staggered_replacements_matches_reference():
+    """Twenty consecutive growth trials with the per-trial tail of chain_growth
+    (:5841-5875), with silent neurons crossing the 1000-trial window at different trials,
+    so that replacements (:15869-15881) fall between growth trials while rows saturate
+    and remodel: the whole state after every trial, and every replacement's positions,
+    connections and delays, the same bits as the reference's."""
+    probe = growth_net(seed=13)
+    train = set(probe.training.tolist())
+    silent = [i for i in range(probe.n_ra) if i not in train][:5]
+    net = growth_net(seed=13)
+    for k, i in enumerate(silent):
+        net.trials_after_replacement[i] = 1000 - 3 * k   # crosses the window after trial 3k
+    o, r = OracleNet(net), RefSimNet(net)
+    events = []
+    for t in range(20):
+        assert o.run_trial(True, t) == 0 and r.run_trial(True, t) == 0
+        n = o.after_growth_trial(t)
+        assert n == r.after_growth_trial(t), t
+        assert_same_state(o, r, t)
+        if n:
+            events.append(t)
+            assert np.array_equal(o.replaced(), r.replaced()), t
+            assert np.array_equal(o.delays(), r.delays()), t
+            for which in (0, 1):
+                for x, y in zip(o.connections(which), r.connections(which)):
+                    assert np.array_equal(x, y), (t, which)
+            for x, y in zip(o.coordinates(), r.coordinates()):
+                assert np.array_equal(x, y), t
+    assert len(events) >= 3, events
+    assert sum(map(len, o.synapse_list(1))) > 0
+    assert o.neuron_props()["remodeled"].sum() > 0
 
 
 def test_config1_growth_matches_reference():
